@@ -1,0 +1,228 @@
+/*
+ * pbf.h — C ABI of the GB300 (sm_103a) Position Based Fluids substep library.
+ *
+ * This is the drop-in boundary for pbf's per-substep simulation path: the
+ * SPH class (src/SPH.h, src/SPH.cpp), its RadixSort (src/RadixSort.h) and its
+ * NeighbourCellFinder (src/NeighbourCellFinder.h).  Every entry point below
+ * names the reference member it replaces.
+ *
+ * Conventions
+ *  - Plain C types only: pointers, sizes, POD structs.  No exceptions cross
+ *    the ABI; every call returns a pbf_status, and pbf_last_error() gives the
+ *    message of the last failure on a handle.
+ *  - The library owns all device memory of a handle (the reference's SPH owns
+ *    its GL buffers, src/SPH.cpp:96-133).  Caller pointers are borrowed for the
+ *    duration of the call only.
+ *  - Particle state crosses the ABI as float4 per particle (x, y, z, w) in
+ *    particle-id order, exactly like the reference's position and velocity
+ *    buffers (src/SPH.h:49,181; shaders/sph/update.glsl:26-27).  The w lane is
+ *    written as 0 and ignored on input.
+ *  - A handle is bound to the CUDA device that was current at creation and
+ *    to one CUDA stream (default: the legacy default stream).  Calls on one
+ *    handle are not thread-safe, matching the reference's single GL context.
+ *  - Stepping is asynchronous.  Device-side failures (non-finite positions, a
+ *    sort lookback that ran out of its spin budget) are latched in a device
+ *    status word and reported by the next synchronising call (pbf_synchronize,
+ *    pbf_get_state, the pbf_get_* debug reads).
+ */
+#ifndef PBF_GB300_PBF_H
+#define PBF_GB300_PBF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PBF_ABI_VERSION 1
+
+typedef enum pbf_status {
+    PBF_OK = 0,
+    PBF_ERR_INVALID_ARGUMENT = 1, /* bad pointer, size or parameter */
+    PBF_ERR_OUT_OF_MEMORY = 2,    /* a device or pinned-host allocation failed */
+    PBF_ERR_CUDA = 3,             /* a CUDA runtime call failed */
+    PBF_ERR_DEVICE_FAULT = 4,     /* the device status word latched an error */
+    PBF_ERR_NO_DEVICE = 5,        /* no CUDA device is visible */
+    PBF_ERR_UNSUPPORTED = 6       /* the request is outside what this build does */
+} pbf_status;
+
+/* Bits of the device status word (pbf_device_status). */
+#define PBF_DEV_NONFINITE 0x1u       /* a predicted or solved position was NaN/Inf */
+#define PBF_DEV_SORT_TIMEOUT 0x2u    /* a radix-sort lookback exceeded its spin limit */
+#define PBF_DEV_RUN_OVER_127 0x4u    /* a 3-cell neighbour run held >= 128 particles; the
+                                        reference's packed 8-bit count
+                                        (shaders/sph/foreachneighbour.glsl:5) would have
+                                        dropped it.  Informational only. */
+
+/* Where a caller pointer lives. */
+#define PBF_HOST 0
+#define PBF_DEVICE 1
+
+/*
+ * Simulation parameters.  The first eight floats are the reference's
+ * sphparams_t uniform block (src/SPH.h:252-285) in the same order; the rest
+ * are the host fields and constants the reference keeps elsewhere.
+ */
+typedef struct pbf_params {
+    float one_over_rho_0;            /* SPH::SetRestDensity stores 1/rho (src/SPH.cpp:166-169) */
+    float epsilon;                   /* SPH::SetCFMEpsilon (src/SPH.h:79) */
+    float gravity;                   /* SPH::SetGravity (src/SPH.h:93) */
+    float timestep;                  /* SPH::SetTimestep (src/SPH.h:107) */
+    float tensile_instability_k;     /* SPH::SetTensileInstabilityK (src/SPH.h:131) */
+    float tensile_instability_scale; /* SPH::SetTensileInstabilityScale (src/SPH.h:144), = 1/Wpoly6(dq) */
+    float xsph_viscosity_c;          /* SPH::SetXSPHViscosity (src/SPH.h:159) */
+    float vorticity_epsilon;         /* SPH::SetVorticityEpsilon (src/SPH.h:175) */
+    float h;                         /* kernel radius; a shader constant in the reference (src/SPH.cpp:58) */
+    uint32_t num_solver_iterations;  /* SPH::SetNumSolverIterations (src/SPH.h:197) */
+    uint32_t vorticity_confinement;  /* SPH::SetVorticityConfinementEnabled (src/SPH.h:220); also gates XSPH */
+    uint32_t external_force;         /* SPH::SetExternalForce (src/SPH.h:230) */
+    uint32_t grid[3];                /* cell grid (x, y, z), the SPH ctor's gridsize (src/SPH.h:40); cell edge = 1 */
+    float wall_lo[3];                /* position clamp box; the reference hard-codes (16,0,16) .. */
+    float wall_hi[3];                /* .. GRID_SIZE-(16,0,16) (shaders/sph/updatepos.glsl:98-100) */
+} pbf_params;
+
+typedef struct pbf_sim pbf_sim;
+
+/* ---- parameters and scenes (host only, no GPU needed) ---------------------- */
+
+/* Reference defaults (src/SPH.cpp:24-26,136-144, src/SPH.h:40) for a grid of
+ * the given size, except h = 1 (one cell edge) so the 27-cell stencil covers
+ * the kernel support.  Walls as in shaders/sph/updatepos.glsl:98-100. */
+pbf_status pbf_params_default(const uint32_t grid[3], pbf_params* out);
+
+/* Poly6 kernel W(r; h) as the reference's host helper SPH::Wpoly6
+ * (src/SPH.cpp:159-164), evaluated in double. */
+double pbf_wpoly6(double r, double h);
+
+/* Poly6 density of an interior point of a cubic lattice of the given spacing,
+ * self term excluded (the neighbour loop skips j == i,
+ * shaders/sph/foreachneighbour.glsl:9), in double. */
+double pbf_rest_density_lattice(double h, double spacing);
+
+/* Seeded block scene: lattice[0] x lattice[1] x lattice[2] particles at
+ * origin + spacing * (i, j, k), each coordinate jittered by U(-jitter, jitter),
+ * velocities U(-vel_uniform, vel_uniform) per component, plus N(0, vel_sigma^2)
+ * when vel_sigma > 0.  Particle ids run x outermost, then z, then y, as in
+ * Simulation::ResetParticleBuffer (src/Simulation.cpp:214-229).  Random
+ * numbers come from a 64-bit Mersenne twister (mt19937_64) with explicit
+ * uniform / Box-Muller transforms, so every platform generates the same bytes.
+ * x4 and v4 receive lattice[0]*lattice[1]*lattice[2] float4 each. */
+pbf_status pbf_scene_block(const uint32_t lattice[3], float spacing, const float origin[3],
+                           float jitter, float vel_uniform, float vel_sigma, uint64_t seed,
+                           float* x4, float* v4);
+
+/* ---- single-scene handle: the SPH class ------------------------------------ */
+
+/* SPH::SPH (src/SPH.h:40, src/SPH.cpp:24-151).  Any n >= 1 (the reference
+ * needs a multiple of 512).  Uses the current CUDA device. */
+pbf_status pbf_create(const pbf_params* params, uint32_t n, pbf_sim** out);
+
+/* SPH::~SPH (src/SPH.h:43, src/SPH.cpp:153-157). */
+void pbf_destroy(pbf_sim* sim);
+
+/* All SPH::Set* parameter setters at once (src/SPH.cpp:166-204, uploaded by
+ * SPH::UploadSPHParams :206-216).  The grid must not change. */
+pbf_status pbf_set_params(pbf_sim* sim, const pbf_params* params);
+pbf_status pbf_get_params(const pbf_sim* sim, pbf_params* out);
+uint32_t pbf_num_particles(const pbf_sim* sim);
+
+/* Binds the handle to a CUDA stream (cudaStream_t passed as void*); NULL is
+ * the legacy default stream. */
+pbf_status pbf_set_stream(pbf_sim* sim, void* stream);
+
+/* Initial particle state, float4 per particle in id order; what the
+ * reference's Simulation::ResetParticleBuffer writes into the SPH buffers
+ * (src/Simulation.cpp:248-268).  where = PBF_HOST or PBF_DEVICE. */
+pbf_status pbf_set_state(pbf_sim* sim, const float* x4, const float* v4, int where);
+
+/* Reads positions / velocities (id order), the contents of
+ * GetPositionBuffer / GetVelocityBuffer (src/SPH.h:49,181).  Either pointer
+ * may be NULL.  Synchronises and reports the device status word. */
+pbf_status pbf_get_state(pbf_sim* sim, float* x4, float* v4, int where);
+
+/* Zero-copy device pointers to the id-order position and velocity arrays
+ * (float4[n]), the CUDA counterpart of the GL buffer names returned by
+ * GetPositionBuffer / GetVelocityBuffer. */
+pbf_status pbf_device_buffers(pbf_sim* sim, float** x4, float** v4);
+
+/* SPH::Run (src/SPH.h:235, src/SPH.cpp:246-334), `substeps` times:
+ * predict, cell keys, stable radix sort, cell ranges, num_solver_iterations
+ * x (lambda, delta-p + wall clamp), velocity commit, and, when
+ * vorticity_confinement is set, XSPH viscosity + vorticity confinement.
+ * Asynchronous on the handle's stream.  After the first call the substep is
+ * replayed from a captured CUDA graph. */
+pbf_status pbf_step(pbf_sim* sim, uint32_t substeps);
+
+/* Waits for the handle's stream and reports the device status word. */
+pbf_status pbf_synchronize(pbf_sim* sim);
+pbf_status pbf_device_status(pbf_sim* sim, uint32_t* bits);
+
+/* Per-phase timers, the counterpart of SPH's GL_TIME_ELAPSED queries
+ * (src/SPH.cpp:218-240): predict, sort, neighbour cells, solver,
+ * commit + vorticity.  When enabled, pbf_step runs the stages eagerly with
+ * CUDA events between them; ms[5] receives the last substep's times. */
+pbf_status pbf_enable_timing(pbf_sim* sim, int enable);
+pbf_status pbf_get_timing(pbf_sim* sim, float ms[5]);
+
+/* ---- debug reads of the last substep's intermediates (synchronising) -------- */
+
+/* Cell key of every particle in id order (the key GetHash computes,
+ * shaders/radixsort/counting.glsl:53-57), sorted keys and the sort
+ * permutation (perm[i] = id of the i-th particle in sorted order,
+ * the w lane of RadixSort's output records).  Any pointer may be NULL. */
+pbf_status pbf_get_sort(pbf_sim* sim, uint32_t* keys_by_id, uint32_t* sorted_keys, uint32_t* perm);
+
+/* Dense cell tables of NeighbourCellFinder (findcells.glsl:34-53):
+ * start[c] = first sorted index in cell c, end[c] = one past its last, both
+ * -1 for empty cells.  Each array has grid[0]*grid[1]*grid[2] entries. */
+pbf_status pbf_get_cells(pbf_sim* sim, int32_t* start, int32_t* end);
+
+/* Lambda of the last solver iteration and the predicted positions (float4,
+ * sorted order) the neighbour runs were built from.  Either may be NULL. */
+pbf_status pbf_get_solver(pbf_sim* sim, float* lambda_sorted, float* xpred4_sorted);
+
+/* ---- standalone stages on caller device buffers ----------------------------- */
+
+/* RadixSort::Run (src/RadixSort.h:57, src/RadixSort.cpp:124-133): stable sort
+ * of n 32-bit keys on their low `numbits` bits (1..32), onesweep with
+ * decoupled lookback.  perm_out[i] = input index of the i-th smallest key,
+ * ties in input order; keys_out (may be NULL) receives the sorted keys.
+ * Device pointers; runs on `stream` and synchronises before returning.
+ * Scratch memory is allocated by the library on first use and cached. */
+pbf_status pbf_radix_sort(const uint32_t* keys_in, uint32_t* keys_out, uint32_t* perm_out,
+                          uint32_t n, uint32_t numbits, void* stream);
+
+/* NeighbourCellFinder's findcells pass (shaders/neighbourcellfinder/findcells.glsl:34-53)
+ * on n sorted keys below num_cells: fills start/end (num_cells entries each,
+ * -1 for empty cells).  Device pointers; synchronises before returning. */
+pbf_status pbf_find_cells(const uint32_t* sorted_keys, uint32_t n, uint32_t num_cells,
+                          int32_t* start, int32_t* end, void* stream);
+
+/* ---- diagnostics ------------------------------------------------------------- */
+
+typedef struct pbf_diagnostics {
+    double mean_density_error; /* mean over particles of |rho_i / rho_0 - 1| */
+    double max_density_error;  /* max over particles of |rho_i / rho_0 - 1| */
+    double kinetic_energy;     /* 0.5 * sum |v|^2, unit mass */
+    double candidate_pairs;    /* sum over particles of (27-cell candidates - 1) */
+} pbf_diagnostics;
+
+/* Density error (self term excluded, as the lambda kernel computes it),
+ * kinetic energy and neighbour-candidate count of the current state, with a
+ * fresh cell sort of the current positions.  Synchronising. */
+pbf_status pbf_compute_diagnostics(pbf_sim* sim, pbf_diagnostics* out);
+
+/* ---- errors ------------------------------------------------------------------ */
+
+const char* pbf_status_string(pbf_status status);
+/* Message of the last failed call on `sim`, or of the last failed call
+ * without a handle when sim is NULL.  Never NULL. */
+const char* pbf_last_error(const pbf_sim* sim);
+int pbf_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PBF_GB300_PBF_H */

@@ -1,0 +1,172 @@
+"""CPU oracle of the PBF substep path — TEST INFRASTRUCTURE ONLY.
+
+A C++ restatement of the reference's GLSL compute shaders (pbf_oracle.hpp),
+FP32 and an FP64 twin, OpenMP-parallel over particles.  Only tests/,
+``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` may use
+it, and only as the checker or the timed CPU baseline: the product
+(pbf_gb300/) never imports, links or calls it.
+
+Parity status: the reference runs only inside an OpenGL 4.3 context, which
+neither machine here has, and it ships no tests or golden vectors.  The
+oracle is pinned by known-answer tests derived from the shader source (kernel
+constants, the rest-lattice density, hand-built sort and cell-range cases)
+and by committed fixtures it generated (tests/golden/), not by outputs of the
+reference itself.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libpbf_oracle.so")
+SRC = [os.path.join(HERE, "pbf_oracle.cpp"), os.path.join(HERE, "pbf_oracle.hpp")]
+
+CXXFLAGS = ["-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"]
+
+
+def build(force: bool = False) -> str:
+    """Compiles the oracle with g++ (no -ffast-math, contraction off)."""
+    os.makedirs(BUILD, exist_ok=True)
+    if not force and os.path.exists(LIB) and all(
+            os.path.getmtime(LIB) >= os.path.getmtime(s) for s in SRC):
+        return LIB
+    tmp = LIB + ".tmp"
+    cmd = [os.environ.get("CXX", "g++")] + CXXFLAGS + ["-o", tmp, SRC[0]]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + " ".join(cmd) + "\n" + r.stderr)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        lib = C.CDLL(LIB)
+        P = C.c_void_p
+        lib.pbfo_params_size.restype = C.c_int
+        lib.pbfo_create.restype = P
+        lib.pbfo_create.argtypes = [P, C.c_uint32, C.c_int, C.c_int]
+        lib.pbfo_destroy.argtypes = [P]
+        lib.pbfo_set_params.argtypes = [P, P]
+        lib.pbfo_set_state.argtypes = [P, P, P]
+        lib.pbfo_get_state.argtypes = [P, P, P]
+        lib.pbfo_step.restype = C.c_double
+        lib.pbfo_step.argtypes = [P, C.c_uint32]
+        lib.pbfo_get_sort.argtypes = [P, P, P, P]
+        lib.pbfo_get_cells.argtypes = [P, P, P]
+        lib.pbfo_get_solver.argtypes = [P, P, P]
+        lib.pbfo_get_runs.argtypes = [P, C.c_uint32, P]
+        lib.pbfo_get_consts.argtypes = [P, P]
+        lib.pbfo_diagnostics.argtypes = [P, P]
+        lib.pbfo_radix_sort.argtypes = [P, C.c_uint32, C.c_uint32, P, P]
+        lib.pbfo_max_threads.restype = C.c_int
+        _lib = lib
+    return _lib
+
+
+def max_threads() -> int:
+    return int(load().pbfo_max_threads())
+
+
+class Oracle:
+    """One oracle simulation (FP32, or the FP64 twin with fp64=True)."""
+
+    def __init__(self, params, n: int, fp64: bool = False, threads: int = 0):
+        self._lib = load()
+        self.fp64 = bool(fp64)
+        self.n = int(n)
+        self._params = params
+        self.ncells = int(params.grid[0]) * int(params.grid[1]) * int(params.grid[2])
+        self._h = self._lib.pbfo_create(C.addressof(params), self.n, int(fp64), int(threads))
+        self._rt = np.float64 if fp64 else np.float32
+
+    def close(self):
+        if self._h:
+            self._lib.pbfo_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, params):
+        self._params = params
+        self._lib.pbfo_set_params(self._h, C.addressof(params))
+
+    def set_state(self, x4, v4):
+        x = np.ascontiguousarray(x4, np.float32)
+        v = np.ascontiguousarray(v4, np.float32)
+        assert x.shape == (self.n, 4) and v.shape == (self.n, 4)
+        self._lib.pbfo_set_state(self._h, x.ctypes.data, v.ctypes.data)
+
+    def get_state(self):
+        x = np.empty((self.n, 4), self._rt)
+        v = np.empty((self.n, 4), self._rt)
+        self._lib.pbfo_get_state(self._h, x.ctypes.data, v.ctypes.data)
+        return x, v
+
+    def step(self, substeps: int = 1) -> float:
+        """Runs substeps; returns wall seconds."""
+        return float(self._lib.pbfo_step(self._h, int(substeps)))
+
+    def get_sort(self):
+        kb = np.empty(self.n, np.uint32)
+        sk = np.empty(self.n, np.uint32)
+        pm = np.empty(self.n, np.uint32)
+        self._lib.pbfo_get_sort(self._h, kb.ctypes.data, sk.ctypes.data, pm.ctypes.data)
+        return kb, sk, pm
+
+    def get_cells(self):
+        st = np.empty(self.ncells, np.int32)
+        en = np.empty(self.ncells, np.int32)
+        self._lib.pbfo_get_cells(self._h, st.ctypes.data, en.ctypes.data)
+        return st, en
+
+    def get_solver(self):
+        lam = np.empty(self.n, self._rt)
+        xp = np.empty((self.n, 4), self._rt)
+        self._lib.pbfo_get_solver(self._h, lam.ctypes.data, xp.ctypes.data)
+        return lam, xp
+
+    def get_runs(self, i: int):
+        r = np.empty(18, np.int32)
+        self._lib.pbfo_get_runs(self._h, int(i), r.ctypes.data)
+        return r.reshape(9, 2)
+
+    def consts(self):
+        out = np.empty(4, np.float64)
+        self._lib.pbfo_get_consts(self._h, out.ctypes.data)
+        return {"k6": out[0], "kg": out[1], "kg_lambda": out[2], "h2": out[3]}
+
+    def diagnostics(self):
+        out = np.empty(4, np.float64)
+        self._lib.pbfo_diagnostics(self._h, out.ctypes.data)
+        return {"mean_density_error": out[0], "max_density_error": out[1],
+                "kinetic_energy": out[2], "candidate_pairs": out[3]}
+
+
+def radix_sort(keys, numbits: int):
+    """Stable sort of keys on their low numbits bits: (sorted keys, perm)."""
+    lib = load()
+    k = np.ascontiguousarray(keys, np.uint32)
+    n = k.shape[0]
+    ko = np.empty(n, np.uint32)
+    po = np.empty(n, np.uint32)
+    lib.pbfo_radix_sort(k.ctypes.data, n, int(numbits), ko.ctypes.data, po.ctypes.data)
+    return ko, po
+
+
+def params_size() -> int:
+    return int(load().pbfo_params_size())

@@ -1,0 +1,618 @@
+// api.cu — the C ABI of include/pbf.h: the pbf_sim handle (the reference's SPH
+// class, src/SPH.h / src/SPH.cpp), its substep pipeline, CUDA-graph replay,
+// debug reads and the standalone sort / cell-finder entry points.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/pbf.h"
+#include "common.cuh"
+#include "sort.cuh"
+#include "substep.cuh"
+
+using namespace pbf;
+
+namespace {
+
+thread_local std::string g_error;  // last error of calls without a handle
+
+}  // namespace
+
+struct pbf_sim {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    pbf_params params{};
+    DevConsts dc{};
+    uint32_t n = 0;
+    uint32_t ncells = 0;
+    uint32_t numbits = 0;
+
+    // id-order state and predicted positions
+    float4 *x = nullptr, *v = nullptr, *xstar = nullptr;
+    // sorted-order buffers
+    float4 *XP = nullptr, *Pa = nullptr, *Pb = nullptr, *L = nullptr;
+    float4 *VS = nullptr, *VX = nullptr, *OM = nullptr, *Q = nullptr;
+    uint32_t *keys = nullptr, *skeys = nullptr, *perm = nullptr;
+    int32_t *cstart = nullptr, *cend = nullptr;
+    uint32_t* status = nullptr;  // device status word [0], bad-key flag [1]
+    uint32_t* h_status = nullptr;
+    void* sort_mem = nullptr;
+    SortWorkspace sort;
+
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool graph_valid = false;
+
+    bool timing = false;
+    cudaEvent_t ev[6] = {};
+    float ms[5] = {};
+
+    std::string err;
+};
+
+namespace {
+
+pbf_status fail(pbf_sim* s, pbf_status st, const std::string& msg) {
+    if (s)
+        s->err = msg;
+    else
+        g_error = msg;
+    return st;
+}
+
+pbf_status cuda_fail(pbf_sim* s, cudaError_t e, const char* what) {
+    std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
+    return fail(s, e == cudaErrorMemoryAllocation ? PBF_ERR_OUT_OF_MEMORY : PBF_ERR_CUDA, msg);
+}
+
+#define PBF_CUDA(s, call)                                   \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail((s), e_, #call); \
+    } while (0)
+
+pbf_status validate_params(const pbf_params* p, std::string& why) {
+    if (!p) {
+        why = "params is NULL";
+        return PBF_ERR_INVALID_ARGUMENT;
+    }
+    if (!(p->h > 0.0f) || !std::isfinite(p->h)) {
+        why = "h must be positive and finite";
+        return PBF_ERR_INVALID_ARGUMENT;
+    }
+    if (!(p->timestep > 0.0f) || !std::isfinite(p->timestep)) {
+        why = "timestep must be positive and finite";
+        return PBF_ERR_INVALID_ARGUMENT;
+    }
+    const float fs[] = {p->one_over_rho_0, p->epsilon, p->gravity, p->tensile_instability_k,
+                        p->tensile_instability_scale, p->xsph_viscosity_c, p->vorticity_epsilon};
+    for (float f : fs)
+        if (!std::isfinite(f)) {
+            why = "parameters must be finite";
+            return PBF_ERR_INVALID_ARGUMENT;
+        }
+    uint64_t cells = 1;
+    for (int a = 0; a < 3; ++a) {
+        if (p->grid[a] == 0 || p->grid[a] > (1u << 24)) {
+            why = "grid extents must be in [1, 2^24]";
+            return PBF_ERR_INVALID_ARGUMENT;
+        }
+        cells *= p->grid[a];
+        if (!(p->wall_lo[a] <= p->wall_hi[a]) || !std::isfinite(p->wall_lo[a]) ||
+            !std::isfinite(p->wall_hi[a])) {
+            why = "wall_lo must be <= wall_hi and finite";
+            return PBF_ERR_INVALID_ARGUMENT;
+        }
+    }
+    if (cells > 0x7FFFFFFFull) {
+        why = "grid has more than 2^31-1 cells";
+        return PBF_ERR_INVALID_ARGUMENT;
+    }
+    return PBF_OK;
+}
+
+// Folds pbf_params into the kernel constants.  The folding is part of the
+// arithmetic contract: one double-precision evaluation, one rounding to float.
+DevConsts make_consts(const pbf_params& p) {
+    constexpr double kPoly6 = 1.56668147106;
+    constexpr double kSpiky = 4.774648292756860;
+    DevConsts c{};
+    const double hd = (double)p.h;
+    double h6 = 1.0, h9 = 1.0;
+    for (int i = 0; i < 6; ++i) h6 *= hd;
+    for (int i = 0; i < 9; ++i) h9 *= hd;
+    c.h = p.h;
+    c.h2 = (float)(hd * hd);
+    float r2 = c.h2;
+    while (std::sqrt(r2) > c.h) r2 = std::nextafter(r2, 0.0f);
+    while (std::sqrt(std::nextafter(r2, INFINITY)) <= c.h) r2 = std::nextafter(r2, INFINITY);
+    c.r2cut = r2;
+    c.k6 = (float)(kPoly6 / h9);
+    c.kg = (float)(-3.0 * kSpiky / h6);
+    c.kg_lambda = (float)((-3.0 * kSpiky / h6) * (double)p.one_over_rho_0);
+    c.oorho = p.one_over_rho_0;
+    c.eps = p.epsilon;
+    c.scale = p.tensile_instability_scale;
+    c.negk = -p.tensile_instability_k;
+    c.cx = p.xsph_viscosity_c;
+    c.dt = p.timestep;
+    volatile float g = p.gravity, dt = p.timestep, ev = p.vorticity_epsilon;
+    c.gdt = g * dt;
+    c.g2dt = (2.0f * g) * dt;
+    c.dteps = dt * ev;
+    for (int a = 0; a < 3; ++a) {
+        c.lo[a] = p.wall_lo[a];
+        c.hi[a] = p.wall_hi[a];
+        c.G[a] = (float)p.grid[a];
+        c.Gi[a] = p.grid[a];
+    }
+    c.half_gz = (float)p.grid[2] / 2.0f;
+    c.GxGz = p.grid[0] * p.grid[2];
+    c.ncells = p.grid[0] * p.grid[1] * p.grid[2];
+    c.ext_force = p.external_force;
+    return c;
+}
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t count) {
+    return cudaMalloc((void**)p, sizeof(T) * (count > 0 ? count : 1));
+}
+
+void free_sim(pbf_sim* s) {
+    if (!s) return;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->exec) cudaGraphExecDestroy(s->exec);
+    if (s->graph) cudaGraphDestroy(s->graph);
+    void* bufs[] = {s->x,  s->v,  s->xstar, s->XP,   s->Pa,     s->Pb,   s->L,
+                    s->VS, s->VX, s->OM,    s->Q,    s->keys,   s->skeys, s->perm,
+                    s->cstart, s->cend, s->status, s->sort_mem};
+    for (void* b : bufs)
+        if (b) cudaFree(b);
+    if (s->h_status) cudaFreeHost(s->h_status);
+    for (cudaEvent_t e : s->ev)
+        if (e) cudaEventDestroy(e);
+    if (s->own_stream) cudaStreamDestroy(s->own_stream);
+    cudaSetDevice(prev);
+    delete s;
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+        else prev = -1;
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+// Final sorted positions of a substep with `iters` solver iterations.
+float4* final_positions(pbf_sim* s, uint32_t iters) {
+    if (iters == 0) return s->XP;
+    return (iters % 2 == 1) ? s->Pa : s->Pb;
+}
+
+// Enqueues one substep (SPH::Run, src/SPH.cpp:246-334) on s->stream.  With
+// `ev` non-null, records an event after each of the five reference phases.
+cudaError_t enqueue_substep(pbf_sim* s, cudaEvent_t* ev) {
+    const uint32_t n = s->n;
+    const unsigned g = grid_for(n);
+    const DevConsts& c = s->dc;
+    cudaStream_t st = s->stream;
+    if (ev) cudaEventRecord(ev[0], st);
+    // 1 predict (predictpos.glsl)
+    k_predict<<<g, kBlock, 0, st>>>(s->x, s->v, s->xstar, s->keys, n, c, s->status);
+    if (ev) cudaEventRecord(ev[1], st);
+    // 2 sort (RadixSort::Run); first clear the cell starts of the previous
+    // substep while its sorted keys are still there
+    k_unmark_cells<<<g, kBlock, 0, st>>>(s->skeys, n, s->ncells, s->cstart);
+    cudaError_t e = sort_pairs(s->sort, s->keys, s->skeys, s->perm, n, s->numbits, s->status, st);
+    if (e != cudaSuccess) return e;
+    if (ev) cudaEventRecord(ev[2], st);
+    // 3 cell ranges (NeighbourCellFinder::FindNeighbourCells)
+    k_find_cells<<<g, kBlock, 0, st>>>(s->skeys, s->perm, s->xstar, s->XP, n, s->ncells, s->cstart,
+                                       s->cend, s->status + 1);
+    if (ev) cudaEventRecord(ev[3], st);
+    // 4 solver iterations (calclambda / updatepos)
+    const float4* cur = s->XP;
+    for (uint32_t it = 0; it < s->params.num_solver_iterations; ++it) {
+        float4* nxt = (it % 2 == 0) ? s->Pa : s->Pb;
+        k_lambda<<<g, kBlock, 0, st>>>(cur, s->skeys, s->cstart, s->cend, s->L, n, c);
+        k_delta_p<<<g, kBlock, 0, st>>>(s->L, s->skeys, s->cstart, s->cend, nxt, n, c, s->status);
+        cur = nxt;
+    }
+    if (ev) cudaEventRecord(ev[4], st);
+    // 5 commit (update.glsl) and XSPH + vorticity (vorticity.glsl)
+    const bool vort = s->params.vorticity_confinement != 0;
+    k_commit<<<g, kBlock, 0, st>>>(cur, s->perm, s->x, s->VS, vort ? nullptr : s->v, n, c);
+    if (vort) {
+        k_vorticity_a<<<g, kBlock, 0, st>>>(cur, s->VS, s->skeys, s->cstart, s->cend, s->VX, s->OM,
+                                            s->Q, n, c);
+        k_vorticity_b<<<g, kBlock, 0, st>>>(s->Q, s->VX, s->OM, s->skeys, s->perm, s->cstart,
+                                            s->cend, s->v, n, c);
+    }
+    if (ev) cudaEventRecord(ev[5], st);
+    return cudaGetLastError();
+}
+
+void invalidate_graph(pbf_sim* s) {
+    if (s->exec) cudaGraphExecDestroy(s->exec);
+    if (s->graph) cudaGraphDestroy(s->graph);
+    s->exec = nullptr;
+    s->graph = nullptr;
+    s->graph_valid = false;
+}
+
+pbf_status check_status(pbf_sim* s) {
+    PBF_CUDA(s, cudaMemcpyAsync(s->h_status, s->status, 2 * sizeof(uint32_t),
+                                cudaMemcpyDeviceToHost, s->stream));
+    PBF_CUDA(s, cudaStreamSynchronize(s->stream));
+    const uint32_t bits = s->h_status[0];
+    if (bits & (kDevNonFinite | kDevSortTimeout)) {
+        std::string m = "device status";
+        if (bits & kDevNonFinite) m += ": non-finite position";
+        if (bits & kDevSortTimeout) m += ": radix-sort lookback timed out";
+        return fail(s, PBF_ERR_DEVICE_FAULT, m);
+    }
+    if (s->h_status[1]) return fail(s, PBF_ERR_DEVICE_FAULT, "device status: cell key out of range");
+    return PBF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+pbf_status pbf_create(const pbf_params* params, uint32_t n, pbf_sim** out) {
+    if (!out) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    std::string why;
+    if (validate_params(params, why) != PBF_OK) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, why);
+    if (n == 0 || n >= (1u << 30)) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "n must be in [1, 2^30)");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(nullptr, PBF_ERR_NO_DEVICE, "no CUDA device");
+    }
+    pbf_sim* s = new pbf_sim();
+    cudaGetDevice(&s->device);
+    s->params = *params;
+    s->dc = make_consts(*params);
+    s->n = n;
+    s->ncells = params->grid[0] * params->grid[1] * params->grid[2];
+    s->numbits = sort_numbits_for_cells(s->ncells);
+    cudaError_t e = cudaSuccess;
+#define ALLOC(ptr, cnt)                                                  \
+    if (e == cudaSuccess) e = dalloc(&s->ptr, (cnt));
+    ALLOC(x, n) ALLOC(v, n) ALLOC(xstar, n) ALLOC(XP, n) ALLOC(Pa, n) ALLOC(Pb, n) ALLOC(L, n)
+    ALLOC(VS, n) ALLOC(VX, n) ALLOC(OM, n) ALLOC(Q, n) ALLOC(keys, n) ALLOC(skeys, n)
+    ALLOC(perm, n) ALLOC(cstart, s->ncells) ALLOC(cend, s->ncells) ALLOC(status, 2)
+#undef ALLOC
+    if (e == cudaSuccess) e = cudaMalloc(&s->sort_mem, SortWorkspace::bytes_for(n));
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&s->h_status, 2 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
+    for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&s->ev[i]);
+    if (e != cudaSuccess) {
+        pbf_status st = cuda_fail(nullptr, e, "pbf_create allocation");
+        free_sim(s);
+        return st;
+    }
+    s->stream = s->own_stream;
+    s->sort.carve(s->sort_mem, n);
+    e = cudaMemsetAsync(s->cstart, 0xFF, sizeof(int32_t) * s->ncells, s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->cend, 0xFF, sizeof(int32_t) * s->ncells, s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->skeys, 0, sizeof(uint32_t) * n, s->stream);
+    // perm always holds ids < n, even if a sort ever fails part-way
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->perm, 0, sizeof(uint32_t) * n, s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->x, 0, sizeof(float4) * n, s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->v, 0, sizeof(float4) * n, s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->status, 0, 2 * sizeof(uint32_t), s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) {
+        pbf_status st = cuda_fail(nullptr, e, "pbf_create initialisation");
+        free_sim(s);
+        return st;
+    }
+    *out = s;
+    return PBF_OK;
+}
+
+void pbf_destroy(pbf_sim* s) { free_sim(s); }
+
+pbf_status pbf_set_params(pbf_sim* s, const pbf_params* p) {
+    if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
+    std::string why;
+    if (validate_params(p, why) != PBF_OK) return fail(s, PBF_ERR_INVALID_ARGUMENT, why);
+    for (int a = 0; a < 3; ++a)
+        if (p->grid[a] != s->params.grid[a])
+            return fail(s, PBF_ERR_INVALID_ARGUMENT, "the grid is fixed at creation");
+    s->params = *p;
+    s->dc = make_consts(*p);
+    invalidate_graph(s);
+    return PBF_OK;
+}
+
+pbf_status pbf_get_params(const pbf_sim* s, pbf_params* out) {
+    if (!s || !out) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = s->params;
+    return PBF_OK;
+}
+
+uint32_t pbf_num_particles(const pbf_sim* s) { return s ? s->n : 0; }
+
+pbf_status pbf_set_stream(pbf_sim* s, void* stream) {
+    if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
+    DeviceGuard dg(s->device);
+    PBF_CUDA(s, cudaStreamSynchronize(s->stream));
+    s->stream = stream ? (cudaStream_t)stream : s->own_stream;
+    return PBF_OK;
+}
+
+pbf_status pbf_set_state(pbf_sim* s, const float* x4, const float* v4, int where) {
+    if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
+    if (!x4 || !v4) return fail(s, PBF_ERR_INVALID_ARGUMENT, "x4 and v4 are required");
+    if (where != PBF_HOST && where != PBF_DEVICE) return fail(s, PBF_ERR_INVALID_ARGUMENT, "bad where");
+    DeviceGuard dg(s->device);
+    const cudaMemcpyKind k = where == PBF_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    PBF_CUDA(s, cudaMemcpyAsync(s->x, x4, sizeof(float4) * s->n, k, s->stream));
+    PBF_CUDA(s, cudaMemcpyAsync(s->v, v4, sizeof(float4) * s->n, k, s->stream));
+    PBF_CUDA(s, cudaStreamSynchronize(s->stream));
+    return PBF_OK;
+}
+
+pbf_status pbf_get_state(pbf_sim* s, float* x4, float* v4, int where) {
+    if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
+    if (where != PBF_HOST && where != PBF_DEVICE) return fail(s, PBF_ERR_INVALID_ARGUMENT, "bad where");
+    DeviceGuard dg(s->device);
+    const cudaMemcpyKind k = where == PBF_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    if (x4) PBF_CUDA(s, cudaMemcpyAsync(x4, s->x, sizeof(float4) * s->n, k, s->stream));
+    if (v4) PBF_CUDA(s, cudaMemcpyAsync(v4, s->v, sizeof(float4) * s->n, k, s->stream));
+    return check_status(s);
+}
+
+pbf_status pbf_device_buffers(pbf_sim* s, float** x4, float** v4) {
+    if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
+    if (x4) *x4 = (float*)s->x;
+    if (v4) *v4 = (float*)s->v;
+    return PBF_OK;
+}
+
+pbf_status pbf_step(pbf_sim* s, uint32_t substeps) {
+    if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
+    DeviceGuard dg(s->device);
+    if (s->timing) {
+        for (uint32_t k = 0; k < substeps; ++k) {
+            cudaError_t e = enqueue_substep(s, s->ev);
+            if (e != cudaSuccess) return cuda_fail(s, e, "substep launch");
+        }
+        if (substeps > 0) {
+            PBF_CUDA(s, cudaEventSynchronize(s->ev[5]));
+            for (int p = 0; p < 5; ++p) cudaEventElapsedTime(&s->ms[p], s->ev[p], s->ev[p + 1]);
+        }
+        return PBF_OK;
+    }
+    if (!s->graph_valid) {
+        invalidate_graph(s);
+        PBF_CUDA(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = enqueue_substep(s, nullptr);
+        cudaGraph_t g = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
+        if (e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return cuda_fail(s, e, "substep capture");
+        }
+        if (e2 != cudaSuccess) return cuda_fail(s, e2, "cudaStreamEndCapture");
+        s->graph = g;
+        PBF_CUDA(s, cudaGraphInstantiate(&s->exec, s->graph, 0));
+        s->graph_valid = true;
+    }
+    for (uint32_t k = 0; k < substeps; ++k) PBF_CUDA(s, cudaGraphLaunch(s->exec, s->stream));
+    return PBF_OK;
+}
+
+pbf_status pbf_synchronize(pbf_sim* s) {
+    if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
+    DeviceGuard dg(s->device);
+    return check_status(s);
+}
+
+pbf_status pbf_device_status(pbf_sim* s, uint32_t* bits) {
+    if (!s || !bits) return fail(s, PBF_ERR_INVALID_ARGUMENT, "NULL argument");
+    DeviceGuard dg(s->device);
+    PBF_CUDA(s, cudaMemcpyAsync(s->h_status, s->status, 2 * sizeof(uint32_t),
+                                cudaMemcpyDeviceToHost, s->stream));
+    PBF_CUDA(s, cudaStreamSynchronize(s->stream));
+    *bits = s->h_status[0];
+    return PBF_OK;
+}
+
+pbf_status pbf_enable_timing(pbf_sim* s, int enable) {
+    if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
+    s->timing = enable != 0;
+    return PBF_OK;
+}
+
+pbf_status pbf_get_timing(pbf_sim* s, float ms[5]) {
+    if (!s || !ms) return fail(s, PBF_ERR_INVALID_ARGUMENT, "NULL argument");
+    for (int p = 0; p < 5; ++p) ms[p] = s->ms[p];
+    return PBF_OK;
+}
+
+pbf_status pbf_get_sort(pbf_sim* s, uint32_t* keys_by_id, uint32_t* sorted_keys, uint32_t* perm) {
+    if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
+    DeviceGuard dg(s->device);
+    const size_t b = sizeof(uint32_t) * s->n;
+    if (keys_by_id) PBF_CUDA(s, cudaMemcpyAsync(keys_by_id, s->keys, b, cudaMemcpyDeviceToHost, s->stream));
+    if (sorted_keys) PBF_CUDA(s, cudaMemcpyAsync(sorted_keys, s->skeys, b, cudaMemcpyDeviceToHost, s->stream));
+    if (perm) PBF_CUDA(s, cudaMemcpyAsync(perm, s->perm, b, cudaMemcpyDeviceToHost, s->stream));
+    return check_status(s);
+}
+
+pbf_status pbf_get_cells(pbf_sim* s, int32_t* start, int32_t* end) {
+    if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
+    DeviceGuard dg(s->device);
+    std::vector<int32_t> st(s->ncells), en(s->ncells);
+    PBF_CUDA(s, cudaMemcpyAsync(st.data(), s->cstart, sizeof(int32_t) * s->ncells,
+                                cudaMemcpyDeviceToHost, s->stream));
+    PBF_CUDA(s, cudaMemcpyAsync(en.data(), s->cend, sizeof(int32_t) * s->ncells,
+                                cudaMemcpyDeviceToHost, s->stream));
+    pbf_status r = check_status(s);
+    if (r != PBF_OK) return r;
+    // cell_end is only maintained where cell_start is set
+    for (uint32_t c = 0; c < s->ncells; ++c)
+        if (st[c] == -1) en[c] = -1;
+    if (start) std::memcpy(start, st.data(), sizeof(int32_t) * s->ncells);
+    if (end) std::memcpy(end, en.data(), sizeof(int32_t) * s->ncells);
+    return PBF_OK;
+}
+
+pbf_status pbf_get_solver(pbf_sim* s, float* lambda_sorted, float* xpred4_sorted) {
+    if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
+    DeviceGuard dg(s->device);
+    if (xpred4_sorted)
+        PBF_CUDA(s, cudaMemcpyAsync(xpred4_sorted, s->XP, sizeof(float4) * s->n,
+                                    cudaMemcpyDeviceToHost, s->stream));
+    if (lambda_sorted) {
+        std::vector<float4> l(s->n);
+        PBF_CUDA(s, cudaMemcpyAsync(l.data(), s->L, sizeof(float4) * s->n, cudaMemcpyDeviceToHost,
+                                    s->stream));
+        pbf_status r = check_status(s);
+        if (r != PBF_OK) return r;
+        for (uint32_t i = 0; i < s->n; ++i) lambda_sorted[i] = l[i].w;
+        return PBF_OK;
+    }
+    return check_status(s);
+}
+
+pbf_status pbf_compute_diagnostics(pbf_sim* s, pbf_diagnostics* out) {
+    if (!s || !out) return fail(s, PBF_ERR_INVALID_ARGUMENT, "NULL argument");
+    DeviceGuard dg(s->device);
+    const uint32_t n = s->n;
+    const unsigned g = grid_for(n);
+    cudaStream_t st = s->stream;
+    k_unmark_cells<<<g, kBlock, 0, st>>>(s->skeys, n, s->ncells, s->cstart);
+    k_keys_of<<<g, kBlock, 0, st>>>(s->x, s->xstar, s->keys, n, s->dc);
+    cudaError_t e = sort_pairs(s->sort, s->keys, s->skeys, s->perm, n, s->numbits, s->status, st);
+    if (e != cudaSuccess) return cuda_fail(s, e, "diagnostics sort");
+    k_find_cells<<<g, kBlock, 0, st>>>(s->skeys, s->perm, s->xstar, s->XP, n, s->ncells, s->cstart,
+                                       s->cend, s->status + 1);
+    k_diagnostics<<<g, kBlock, 0, st>>>(s->XP, s->v, s->skeys, s->perm, s->cstart, s->cend, s->VX,
+                                        n, s->dc);
+    PBF_CUDA(s, cudaGetLastError());
+    std::vector<float4> h(n);
+    PBF_CUDA(s, cudaMemcpyAsync(h.data(), s->VX, sizeof(float4) * n, cudaMemcpyDeviceToHost, st));
+    pbf_status r = check_status(s);
+    if (r != PBF_OK) return r;
+    double se = 0, me = 0, ke = 0, cand = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        se += h[i].x;
+        me = me > h[i].x ? me : h[i].x;
+        ke += h[i].y;
+        cand += h[i].z;
+    }
+    out->mean_density_error = se / n;
+    out->max_density_error = me;
+    out->kinetic_energy = ke;
+    out->candidate_pairs = cand;
+    return PBF_OK;
+}
+
+// ---- standalone stages ------------------------------------------------------
+
+namespace {
+
+struct CachedSortScratch {
+    void* mem = nullptr;
+    uint32_t capacity = 0;
+    uint32_t* keys_scratch = nullptr;
+    uint32_t* status = nullptr;
+    SortWorkspace ws;
+};
+std::mutex g_scratch_mu;
+std::map<int, CachedSortScratch> g_scratch;
+
+}  // namespace
+
+pbf_status pbf_radix_sort(const uint32_t* keys_in, uint32_t* keys_out, uint32_t* perm_out,
+                          uint32_t n, uint32_t numbits, void* stream) {
+    if (n == 0) return PBF_OK;
+    if (!keys_in || !perm_out) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "keys_in and perm_out are required");
+    if (n >= (1u << 30)) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "n must be below 2^30");
+    if (numbits < 1 || numbits > 32) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "numbits must be in [1, 32]");
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return fail(nullptr, PBF_ERR_NO_DEVICE, "no CUDA device");
+    cudaStream_t st = (cudaStream_t)stream;
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    CachedSortScratch& c = g_scratch[dev];
+    if (c.capacity < n) {
+        if (c.mem) {
+            cudaDeviceSynchronize();
+            cudaFree(c.mem);
+            c.mem = nullptr;
+            c.capacity = 0;
+        }
+        const size_t wsb = (SortWorkspace::bytes_for(n) + 255) & ~size_t(255);
+        const size_t bytes = wsb + sizeof(uint32_t) * (size_t)n + 256;
+        cudaError_t e = cudaMalloc(&c.mem, bytes);
+        if (e != cudaSuccess) return cuda_fail(nullptr, e, "sort scratch allocation");
+        c.capacity = n;
+        c.ws.carve(c.mem, n);
+        c.keys_scratch = (uint32_t*)((uint8_t*)c.mem + wsb);
+        c.status = (uint32_t*)((uint8_t*)c.keys_scratch + sizeof(uint32_t) * (size_t)n);
+    }
+    // The sort reads its key buffer once per pass; keys_out must not alias keys_in.
+    uint32_t* kout = keys_out ? keys_out : c.keys_scratch;
+    if ((const void*)kout == (const void*)keys_in || (const void*)perm_out == (const void*)keys_in)
+        return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "outputs must not alias keys_in");
+    cudaError_t e = cudaMemsetAsync(c.status, 0, sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = sort_pairs(c.ws, keys_in, kout, perm_out, n, numbits, c.status, st);
+    uint32_t bits = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bits, c.status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "pbf_radix_sort");
+    if (bits & kDevSortTimeout) return fail(nullptr, PBF_ERR_DEVICE_FAULT, "radix-sort lookback timed out");
+    return PBF_OK;
+}
+
+pbf_status pbf_find_cells(const uint32_t* sorted_keys, uint32_t n, uint32_t num_cells, int32_t* start,
+                          int32_t* end, void* stream) {
+    if (!start || !end || num_cells == 0) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "start, end and num_cells are required");
+    if (n > 0 && !sorted_keys) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sorted_keys is NULL");
+    if (num_cells > 0x7FFFFFFFu || n > 0x7FFFFFFFu) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sizes above 2^31-1");
+    cudaStream_t st = (cudaStream_t)stream;
+    uint32_t* bad = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&bad, sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(start, 0xFF, sizeof(int32_t) * (size_t)num_cells, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(end, 0xFF, sizeof(int32_t) * (size_t)num_cells, st);
+    if (e == cudaSuccess && n > 0) {
+        k_find_cells<<<grid_for(n), kBlock, 0, st>>>(sorted_keys, nullptr, nullptr, nullptr, n,
+                                                     num_cells, start, end, bad);
+        e = cudaGetLastError();
+    }
+    uint32_t hbad = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hbad, bad, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (bad) cudaFreeAsync(bad, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "pbf_find_cells");
+    if (hbad) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "a sorted key is >= num_cells");
+    return PBF_OK;
+}
+
+const char* pbf_last_error(const pbf_sim* s) {
+    if (s) return s->err.c_str();
+    return g_error.c_str();
+}
+
+}  // extern "C"

@@ -1,0 +1,308 @@
+// substep.cu — the per-substep stage kernels of the PBF path.
+//
+// Data layout in HBM (one handle, n particles):
+//   x, v          float4[n]  id order; the drop-in state (SPH position/velocity buffers)
+//   xstar         float4[n]  predicted positions, id order (predictpos output)
+//   keys          u32[n]     cell key per id; sorted keys + perm after the sort
+//   P0, P1        float4[n]  sorted-order Jacobi position buffers (w = 0)
+//   L             float4[n]  sorted (x, y, z, lambda): one 16-byte load per neighbour in delta-p
+//   VS            float4[n]  committed velocity, sorted order
+//   VX, OM        float4[n]  velocity after XSPH / vorticity vector, sorted order
+//   Q             float4[n]  sorted (x, y, z, |vorticity|) for the confinement pass
+//   cell_start    i32[cells] first sorted index of each cell, -1 when empty
+//   cell_end      i32[cells] one past the last sorted index (valid where start != -1)
+//
+// Every neighbour sweep visits, for sorted particle i, the 9 (dy, dz) rows of
+// its 3x3x3 stencil in the reference's order (neighbourcells.glsl:37-47),
+// each row's up-to-3-cell x-run in ascending sorted index, skipping i itself
+// (foreachneighbour.glsl:1-10), and accumulates in that order.
+#include "substep.cuh"
+
+namespace pbf {
+
+namespace {
+
+// Sorted-index ranges of the 9 stencil rows of a cell (neighbourcells.glsl:52-90).
+struct Runs {
+    int32_t b[9], e[9];
+};
+
+__device__ __forceinline__ void runs_of(uint32_t key, const DevConsts& c,
+                                        const int32_t* __restrict__ cstart,
+                                        const int32_t* __restrict__ cend, Runs& r) {
+    const uint32_t Gx = c.Gi[0], Gy = c.Gi[1], Gz = c.Gi[2];
+    const int cx = (int)(key % Gx);
+    const uint32_t rem = key / Gx;
+    const int cz = (int)(rem % Gz);
+    const int cy = (int)(rem / Gz);
+    const int xlo = cx > 0 ? cx - 1 : 0;
+    const int xhi = cx + 1 < (int)Gx ? cx + 1 : (int)Gx - 1;
+#pragma unroll
+    for (int o = 0; o < 9; ++o) {
+        const int ny = cy + (o / 3) - 1, nz = cz + (o % 3) - 1;
+        int32_t first = -1, last = -1;
+        if (ny >= 0 && ny < (int)Gy && nz >= 0 && nz < (int)Gz) {
+            const uint32_t base = (uint32_t)ny * c.GxGz + (uint32_t)nz * Gx;
+            for (int xx = xlo; xx <= xhi; ++xx) {
+                const int32_t s = __ldg(cstart + base + (uint32_t)xx);
+                if (s != -1) {
+                    if (first == -1) first = s;
+                    last = __ldg(cend + base + (uint32_t)xx);
+                }
+            }
+        }
+        r.b[o] = first == -1 ? 0 : first;
+        r.e[o] = first == -1 ? 0 : last;
+    }
+}
+
+}  // namespace
+
+// predictpos.glsl:18-38 fused with the cell key of GetHash (counting.glsl:53-57).
+__global__ void __launch_bounds__(kBlock)
+k_predict(const float4* __restrict__ x, const float4* __restrict__ v, float4* __restrict__ xstar,
+          uint32_t* __restrict__ keys, uint32_t n, DevConsts c, uint32_t* status) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 q = x[i];
+    const float4 w = v[i];
+    float wz = w.z;
+    if (c.ext_force && q.z > c.half_gz) wz = fsub(wz, c.g2dt);  // :27-28
+    const float wy = fsub(w.y, c.gdt);                             // :32
+    const float3 s = make_float3(fadd(q.x, fmul(c.dt, w.x)), fadd(q.y, fmul(c.dt, wy)),
+                                 fadd(q.z, fmul(c.dt, wz)));       // :34
+    if (!finite3(s)) atomicOr(status, kDevNonFinite);
+    xstar[i] = make_float4(s.x, s.y, s.z, 0.0f);
+    keys[i] = cell_key(s, c);
+}
+
+// Cell keys of the current positions (no prediction), for diagnostics.
+__global__ void __launch_bounds__(kBlock)
+k_keys_of(const float4* __restrict__ x, float4* __restrict__ xstar, uint32_t* __restrict__ keys,
+          uint32_t n, DevConsts c) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 q = x[i];
+    xstar[i] = make_float4(q.x, q.y, q.z, 0.0f);
+    keys[i] = cell_key(xyz(q), c);
+}
+
+// Clears the cell-start entries the previous sort set (its sorted keys are
+// still in `prev_sorted`), so the dense table never needs a full memset.
+__global__ void __launch_bounds__(kBlock)
+k_unmark_cells(const uint32_t* __restrict__ prev_sorted, uint32_t n, uint32_t ncells,
+               int32_t* __restrict__ cstart) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t k = prev_sorted[i];
+    if (k < ncells && (i == 0 || prev_sorted[i - 1] != k)) cstart[k] = -1;
+}
+
+// findcells.glsl:34-53 (start of cell(x_0) = 0 and end of cell(x_{n-1}) = n)
+// fused with the gather of the predicted positions into sorted order.
+// Keys >= ncells are skipped and reported through `status` (bad input only).
+__global__ void __launch_bounds__(kBlock)
+k_find_cells(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
+             const float4* __restrict__ xstar, float4* __restrict__ P0, uint32_t n, uint32_t ncells,
+             int32_t* __restrict__ cstart, int32_t* __restrict__ cend, uint32_t* bad) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t k = skeys[i];
+    if (P0) P0[i] = __ldg(xstar + perm[i]);
+    if (k >= ncells) {
+        atomicOr(bad, 1u);
+        return;
+    }
+    if (i == 0 || skeys[i - 1] != k) cstart[k] = (int32_t)i;
+    if (i + 1 == n || skeys[i + 1] != k) cend[k] = (int32_t)(i + 1);
+}
+
+// calclambda.glsl:66-102.  Reads positions P, writes L[i] = (p_i, lambda_i).
+__global__ void __launch_bounds__(kBlock)
+k_lambda(const float4* __restrict__ P, const uint32_t* __restrict__ skeys,
+         const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
+         float4* __restrict__ L, uint32_t n, DevConsts c) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Runs r;
+    runs_of(skeys[i], c, cstart, cend, r);
+    const float3 pi = xyz(P[i]);
+    float rho = 0.0f, sumk = 0.0f;
+    float3 gi = make_float3(0.0f, 0.0f, 0.0f);
+    for (int o = 0; o < 9; ++o) {
+        for (int32_t j = r.b[o]; j < r.e[o]; ++j) {
+            if ((uint32_t)j == i) continue;
+            const float3 d = sub3(pi, xyz(__ldg(P + j)));
+            const float r2 = dot3(d, d);
+            if (r2 > c.r2cut) continue;  // len > h: Wpoly6 = gradWspiky = 0
+            const float len = fsqrt(r2);
+            rho = fadd(rho, w_poly6(c, len));  // :80-82
+            if (len == 0.0f) continue;         // gradWspiky(0) = 0 (:60)
+            const float3 g = scale3(d, grad_scale(c.kg_lambda, c.h, len));  // :86-87
+            sumk = fadd(sumk, dot3(g, g));     // :89
+            gi = add3(gi, g);                  // :93
+        }
+    }
+    sumk = fadd(sumk, dot3(gi, gi));               // :97
+    const float Ci = ffma(rho, c.oorho, -1.0f);    // :100
+    const float lam = fdiv(-Ci, fadd(sumk, c.eps));  // :101
+    L[i] = make_float4(pi.x, pi.y, pi.z, lam);
+}
+
+// updatepos.glsl:42-104.  Reads L = (p, lambda), writes clamped positions Pn.
+__global__ void __launch_bounds__(kBlock)
+k_delta_p(const float4* __restrict__ L, const uint32_t* __restrict__ skeys,
+          const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
+          float4* __restrict__ Pn, uint32_t n, DevConsts c, uint32_t* status) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Runs r;
+    runs_of(skeys[i], c, cstart, cend, r);
+    const float4 Li = L[i];
+    const float3 pi = xyz(Li);
+    const float li = Li.w;
+    float3 dp = make_float3(0.0f, 0.0f, 0.0f);
+    for (int o = 0; o < 9; ++o) {
+        for (int32_t j = r.b[o]; j < r.e[o]; ++j) {
+            if ((uint32_t)j == i) continue;
+            const float4 Lj = __ldg(L + j);
+            const float3 d = sub3(pi, xyz(Lj));
+            const float r2 = dot3(d, d);
+            if (r2 > c.r2cut) continue;
+            const float len = fsqrt(r2);
+            if (len == 0.0f) continue;
+            float sc = fmul(c.scale, w_poly6(c, len));  // :57
+            sc = fmul(sc, sc);                           // :58
+            sc = fmul(sc, sc);                           // :59
+            sc = fmul(c.negk, sc);                       // :60
+            const float coef = fadd(fadd(li, Lj.w), sc); // :65
+            const float3 g = scale3(d, grad_scale(c.kg, c.h, len));
+            dp = fma3(coef, g, dp);                      // :65
+        }
+    }
+    float3 q = fma3(c.oorho, dp, pi);  // :85
+    // clamp (:100) as min(max(q, lo), hi) with explicit selects, so signed
+    // zeros and NaN behave like the oracle's std::min/std::max
+    q.x = (q.x < c.lo[0]) ? c.lo[0] : q.x;
+    q.x = (c.hi[0] < q.x) ? c.hi[0] : q.x;
+    q.y = (q.y < c.lo[1]) ? c.lo[1] : q.y;
+    q.y = (c.hi[1] < q.y) ? c.hi[1] : q.y;
+    q.z = (q.z < c.lo[2]) ? c.lo[2] : q.z;
+    q.z = (c.hi[2] < q.z) ? c.hi[2] : q.z;
+    if (!finite3(q)) atomicOr(status, kDevNonFinite);
+    Pn[i] = make_float4(q.x, q.y, q.z, 0.0f);
+}
+
+// update.glsl:16-28: v = (x* - x_old) / dt, x = x*, scattered back to id order.
+// VS receives the committed velocity in sorted order; when `v_out` is set the
+// velocity is also stored in id order (vorticity confinement disabled).
+__global__ void __launch_bounds__(kBlock)
+k_commit(const float4* __restrict__ P, const uint32_t* __restrict__ perm, float4* __restrict__ x,
+         float4* __restrict__ VS, float4* __restrict__ v_out, uint32_t n, DevConsts c) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t id = perm[i];
+    const float4 q = P[i];
+    const float4 xo = x[id];
+    const float4 w = make_float4(fdiv(fsub(q.x, xo.x), c.dt), fdiv(fsub(q.y, xo.y), c.dt),
+                                 fdiv(fsub(q.z, xo.z), c.dt), 0.0f);  // :23
+    VS[i] = w;
+    x[id] = make_float4(q.x, q.y, q.z, 0.0f);  // :26
+    if (v_out) v_out[id] = w;                  // :27
+}
+
+// vorticity.glsl:34-60: XSPH velocity and the vorticity vector, Jacobi
+// (every read sees the committed velocities).
+__global__ void __launch_bounds__(kBlock)
+k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ VS,
+              const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cstart,
+              const int32_t* __restrict__ cend, float4* __restrict__ VX, float4* __restrict__ OM,
+              float4* __restrict__ Q, uint32_t n, DevConsts c) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Runs r;
+    runs_of(skeys[i], c, cstart, cend, r);
+    const float3 pi = xyz(P[i]);
+    const float3 vi = xyz(VS[i]);
+    float3 acc = make_float3(0.0f, 0.0f, 0.0f), w = make_float3(0.0f, 0.0f, 0.0f);
+    for (int o = 0; o < 9; ++o) {
+        for (int32_t j = r.b[o]; j < r.e[o]; ++j) {
+            if ((uint32_t)j == i) continue;
+            const float3 d = sub3(pi, xyz(__ldg(P + j)));  // :51
+            const float r2 = dot3(d, d);
+            if (r2 > c.r2cut) continue;
+            const float len = fsqrt(r2);
+            const float3 vij = sub3(xyz(__ldg(VS + j)), vi);  // :50
+            acc = fma3(w_poly6(c, len), vij, acc);            // :52-54
+            if (len == 0.0f) continue;
+            const float3 g = scale3(d, grad_scale(c.kg, c.h, len));
+            w = add3(w, cross3(vij, g));  // :55
+        }
+    }
+    const float3 vx = fma3(c.cx, acc, vi);  // :58
+    VX[i] = make_float4(vx.x, vx.y, vx.z, 0.0f);
+    OM[i] = make_float4(w.x, w.y, w.z, 0.0f);
+    Q[i] = make_float4(pi.x, pi.y, pi.z, fsqrt(dot3(w, w)));  // :60
+}
+
+// vorticity.glsl:65-85: confinement from the gradient of |vorticity|; writes
+// the final velocity in id order.
+__global__ void __launch_bounds__(kBlock)
+k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ VX,
+              const float4* __restrict__ OM, const uint32_t* __restrict__ skeys,
+              const uint32_t* __restrict__ perm, const int32_t* __restrict__ cstart,
+              const int32_t* __restrict__ cend, float4* __restrict__ v, uint32_t n, DevConsts c) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Runs r;
+    runs_of(skeys[i], c, cstart, cend, r);
+    const float3 pi = xyz(Q[i]);
+    float3 eta = make_float3(0.0f, 0.0f, 0.0f);
+    for (int o = 0; o < 9; ++o) {
+        for (int32_t j = r.b[o]; j < r.e[o]; ++j) {
+            if ((uint32_t)j == i) continue;
+            const float4 Qj = __ldg(Q + j);
+            const float3 d = sub3(pi, xyz(Qj));  // :69
+            const float r2 = dot3(d, d);
+            if (r2 > c.r2cut) continue;
+            const float len = fsqrt(r2);
+            if (len == 0.0f) continue;
+            eta = fma3(Qj.w, scale3(d, grad_scale(c.kg, c.h, len)), eta);  // :72
+        }
+    }
+    const float l = fsqrt(dot3(eta, eta));  // :76
+    if (l > 0.0f) eta = make_float3(fdiv(eta.x, l), fdiv(eta.y, l), fdiv(eta.z, l));  // :77-78
+    const float3 vf = fma3(c.dteps, cross3(eta, xyz(OM[i])), xyz(VX[i]));  // :82
+    v[perm[i]] = make_float4(vf.x, vf.y, vf.z, 0.0f);                     // :85
+}
+
+// Per-particle density error |rho/rho0 - 1| (self excluded) and kinetic
+// energy of the state sorted into P (positions) with velocities v (id order).
+__global__ void __launch_bounds__(kBlock)
+k_diagnostics(const float4* __restrict__ P, const float4* __restrict__ v,
+              const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
+              const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
+              float4* __restrict__ out, uint32_t n, DevConsts c) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Runs r;
+    runs_of(skeys[i], c, cstart, cend, r);
+    const float3 pi = xyz(P[i]);
+    float rho = 0.0f;
+    int32_t cand = -1;
+    for (int o = 0; o < 9; ++o) {
+        cand += r.e[o] - r.b[o];
+        for (int32_t j = r.b[o]; j < r.e[o]; ++j) {
+            if ((uint32_t)j == i) continue;
+            const float3 d = sub3(pi, xyz(__ldg(P + j)));
+            const float r2 = dot3(d, d);
+            if (r2 > c.r2cut) continue;
+            rho = fadd(rho, w_poly6(c, fsqrt(r2)));
+        }
+    }
+    const float4 w = v[perm[i]];
+    out[i] = make_float4(fabsf(ffma(rho, c.oorho, -1.0f)),
+                         0.5f * (w.x * w.x + w.y * w.y + w.z * w.z), (float)cand, 0.0f);
+}
+
+}  // namespace pbf

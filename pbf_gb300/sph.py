@@ -1,0 +1,258 @@
+"""Python mirror of the reference's ``SPH`` class (src/SPH.h) over the C ABI.
+
+Method names, argument meaning and defaults follow src/SPH.h:40-235 so code
+written against the reference reads the same:
+
+    sph = SPH(numparticles, gridsize=(128, 64, 128))
+    sph.SetRestDensity(rho0); sph.SetNumSolverIterations(4)
+    sph.set_state(x4, v4)        # what Simulation::ResetParticleBuffer uploads
+    sph.Run()                    # one substep (SPH::Run)
+    x4 = sph.positions()         # contents of GetPositionBuffer
+
+Errors raise :class:`PbfError` carrying the C status code.  All compute runs
+in libpbf_gb300.so on the GPU; this module only marshals arguments.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._capi import (PBF_DEVICE, PBF_HOST, Diagnostics, Params, PbfError, check, load)
+
+
+def default_params(gridsize=(128, 64, 128)) -> Params:
+    """Reference defaults (src/SPH.cpp:136-144) for a grid, h = 1."""
+    lib = load()
+    p = Params()
+    g = (C.c_uint32 * 3)(*[int(v) for v in gridsize])
+    check(lib.pbf_params_default(g, C.byref(p)))
+    return p
+
+
+def _f32(v) -> float:
+    return float(np.float32(v))
+
+
+def _as_f4(a, n: int) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if a.shape == (n, 3):
+        a = np.ascontiguousarray(np.concatenate([a, np.zeros((n, 1), np.float32)], axis=1))
+    if a.shape != (n, 4):
+        raise ValueError(f"expected shape ({n}, 4) or ({n}, 3), got {a.shape}")
+    return a
+
+
+class SPH:
+    """One simulation handle (``pbf_sim``), the counterpart of ``SPH``."""
+
+    def __init__(self, numparticles: int, gridsize=(128, 64, 128), params: Params | None = None):
+        self._lib = load()
+        p = params.copy() if params is not None else default_params(gridsize)
+        if params is not None and tuple(p.grid) != tuple(int(g) for g in gridsize):
+            gridsize = tuple(p.grid)
+        self._params = p
+        self._n = int(numparticles)
+        h = C.c_void_p()
+        check(self._lib.pbf_create(C.byref(p), self._n, C.byref(h)))
+        self._h = h
+
+    # ---- lifetime --------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.pbf_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    @property
+    def numparticles(self) -> int:
+        return self._n
+
+    @property
+    def params(self) -> Params:
+        return self._params.copy()
+
+    def set_params(self, p: Params) -> None:
+        check(self._lib.pbf_set_params(self._h, C.byref(p)), self._h)
+        self._params = p.copy()
+
+    def _update(self, **kw) -> None:
+        p = self._params.copy()
+        for k, v in kw.items():
+            setattr(p, k, v)
+        self.set_params(p)
+
+    # ---- reference setters / getters (src/SPH.h:57-230) -------------------
+    def GetRestDensity(self) -> float:
+        return _f32(np.float32(1.0) / np.float32(self._params.one_over_rho_0))
+
+    def SetRestDensity(self, rho: float) -> None:
+        self._update(one_over_rho_0=_f32(np.float32(1.0) / np.float32(rho)))
+
+    def GetCFMEpsilon(self) -> float:
+        return self._params.epsilon
+
+    def SetCFMEpsilon(self, eps: float) -> None:
+        self._update(epsilon=_f32(eps))
+
+    def GetGravity(self) -> float:
+        return self._params.gravity
+
+    def SetGravity(self, g: float) -> None:
+        self._update(gravity=_f32(g))
+
+    def GetTimestep(self) -> float:
+        return self._params.timestep
+
+    def SetTimestep(self, dt: float) -> None:
+        self._update(timestep=_f32(dt))
+
+    def GetTensileInstabilityK(self) -> float:
+        return self._params.tensile_instability_k
+
+    def SetTensileInstabilityK(self, k: float) -> None:
+        self._update(tensile_instability_k=_f32(k))
+
+    def GetTensileInstabilityScale(self) -> float:
+        return self._params.tensile_instability_scale
+
+    def SetTensileInstabilityScale(self, v: float) -> None:
+        self._update(tensile_instability_scale=_f32(v))
+
+    def GetXSPHViscosity(self) -> float:
+        return self._params.xsph_viscosity_c
+
+    def SetXSPHViscosity(self, c: float) -> None:
+        self._update(xsph_viscosity_c=_f32(c))
+
+    def GetVorticityEpsilon(self) -> float:
+        return self._params.vorticity_epsilon
+
+    def SetVorticityEpsilon(self, eps: float) -> None:
+        self._update(vorticity_epsilon=_f32(eps))
+
+    def GetNumSolverIterations(self) -> int:
+        return int(self._params.num_solver_iterations)
+
+    def SetNumSolverIterations(self, it: int) -> None:
+        self._update(num_solver_iterations=int(it))
+
+    def IsVorticityConfinementEnabled(self) -> bool:
+        return bool(self._params.vorticity_confinement)
+
+    def SetVorticityConfinementEnabled(self, flag: bool) -> None:
+        self._update(vorticity_confinement=1 if flag else 0)
+
+    def SetExternalForce(self, state: bool) -> None:
+        self._update(external_force=1 if state else 0)
+
+    # ---- state ------------------------------------------------------------
+    def set_state(self, x4, v4) -> None:
+        """Uploads positions and velocities (id order, (n,4) or (n,3) float32)."""
+        x = _as_f4(x4, self._n)
+        v = _as_f4(v4, self._n)
+        check(self._lib.pbf_set_state(self._h, x.ctypes.data, v.ctypes.data, PBF_HOST), self._h)
+
+    def set_state_device(self, x_ptr: int, v_ptr: int) -> None:
+        check(self._lib.pbf_set_state(self._h, x_ptr, v_ptr, PBF_DEVICE), self._h)
+
+    def get_state(self) -> tuple[np.ndarray, np.ndarray]:
+        x = np.empty((self._n, 4), np.float32)
+        v = np.empty((self._n, 4), np.float32)
+        check(self._lib.pbf_get_state(self._h, x.ctypes.data, v.ctypes.data, PBF_HOST), self._h)
+        return x, v
+
+    def get_state_into(self, x_ptr, v_ptr, where=PBF_HOST) -> None:
+        check(self._lib.pbf_get_state(self._h, x_ptr, v_ptr, where), self._h)
+
+    def positions(self) -> np.ndarray:
+        return self.get_state()[0]
+
+    def velocities(self) -> np.ndarray:
+        return self.get_state()[1]
+
+    def GetPositionBuffer(self) -> int:
+        """Device address of the id-order float4 position array."""
+        x = C.c_void_p()
+        check(self._lib.pbf_device_buffers(self._h, C.byref(x), None), self._h)
+        return int(x.value)
+
+    def GetVelocityBuffer(self) -> int:
+        """Device address of the id-order float4 velocity array."""
+        v = C.c_void_p()
+        check(self._lib.pbf_device_buffers(self._h, None, C.byref(v)), self._h)
+        return int(v.value)
+
+    # ---- stepping -----------------------------------------------------------
+    def Run(self) -> None:
+        """One substep (SPH::Run, src/SPH.cpp:246-334); asynchronous."""
+        check(self._lib.pbf_step(self._h, 1), self._h)
+
+    def step(self, substeps: int) -> None:
+        check(self._lib.pbf_step(self._h, int(substeps)), self._h)
+
+    def synchronize(self) -> None:
+        check(self._lib.pbf_synchronize(self._h), self._h)
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        check(self._lib.pbf_set_stream(self._h, stream_ptr), self._h)
+
+    def device_status(self) -> int:
+        bits = C.c_uint32()
+        check(self._lib.pbf_device_status(self._h, C.byref(bits)), self._h)
+        return int(bits.value)
+
+    # ---- timing (SPH::OutputTiming, src/SPH.cpp:218-240) ---------------------
+    def EnableTiming(self, enable: bool = True) -> None:
+        check(self._lib.pbf_enable_timing(self._h, 1 if enable else 0), self._h)
+
+    def OutputTiming(self) -> dict:
+        ms = (C.c_float * 5)()
+        check(self._lib.pbf_get_timing(self._h, ms), self._h)
+        names = ("predict", "sort", "neighbour_cells", "solver", "vorticity")
+        return {k: float(v) for k, v in zip(names, ms)}
+
+    # ---- debug reads of the last substep ---------------------------------------
+    def get_sort(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        kb = np.empty(self._n, np.uint32)
+        sk = np.empty(self._n, np.uint32)
+        pm = np.empty(self._n, np.uint32)
+        check(self._lib.pbf_get_sort(self._h, kb.ctypes.data, sk.ctypes.data, pm.ctypes.data),
+              self._h)
+        return kb, sk, pm
+
+    def get_cells(self) -> tuple[np.ndarray, np.ndarray]:
+        nc = int(np.prod([int(g) for g in self._params.grid]))
+        st = np.empty(nc, np.int32)
+        en = np.empty(nc, np.int32)
+        check(self._lib.pbf_get_cells(self._h, st.ctypes.data, en.ctypes.data), self._h)
+        return st, en
+
+    def get_solver(self) -> tuple[np.ndarray, np.ndarray]:
+        lam = np.empty(self._n, np.float32)
+        xp = np.empty((self._n, 4), np.float32)
+        check(self._lib.pbf_get_solver(self._h, lam.ctypes.data, xp.ctypes.data), self._h)
+        return lam, xp
+
+    def diagnostics(self) -> dict:
+        d = Diagnostics()
+        check(self._lib.pbf_compute_diagnostics(self._h, C.byref(d)), self._h)
+        return {name: getattr(d, name) for name, _ in Diagnostics._fields_}
+
+
+__all__ = ["SPH", "default_params", "PbfError"]

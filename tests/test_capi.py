@@ -1,0 +1,95 @@
+"""CPU tests of the C ABI: the library loads, exports every entry point that
+include/pbf.h declares, and its host-only functions behave."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from pbf_gb300 import _capi, scenes
+from tests.conftest import HAS_GPU, ROOT
+
+
+def declared_functions():
+    names = []
+    for path in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if not path.endswith(".h"):
+            continue
+        text = open(os.path.join(ROOT, "include", path)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names += re.findall(r"^[A-Za-z_][\w\s\*]*?\b(pbf_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_every_declared_symbol_is_exported(product_lib):
+    names = declared_functions()
+    assert len(names) >= 25
+    for name in names:
+        assert hasattr(product_lib, name), name
+    # and the Python binding covers every declaration
+    assert set(names) <= set(_capi.SIGNATURES), set(names) - set(_capi.SIGNATURES)
+
+
+def test_abi_version_and_status_strings(product_lib):
+    assert product_lib.pbf_abi_version() == 1
+    assert product_lib.pbf_status_string(0) == b"ok"
+    assert product_lib.pbf_status_string(1) == b"invalid argument"
+
+
+def test_params_default_mirrors_reference(product_lib):
+    p = _capi.Params()
+    assert product_lib.pbf_params_default((C.c_uint32 * 3)(128, 64, 128), C.byref(p)) == 0
+    # src/SPH.cpp:136-144 and src/SPH.cpp:25-26
+    assert (p.one_over_rho_0, p.epsilon, p.gravity) == (1.0, 5.0, 10.0)
+    assert p.timestep == np.float32(0.016)
+    assert p.num_solver_iterations == 5 and p.vorticity_confinement == 0
+    assert list(p.wall_lo) == [16.0, 0.0, 16.0] and list(p.wall_hi) == [112.0, 64.0, 112.0]
+    assert product_lib.pbf_params_default((C.c_uint32 * 3)(0, 1, 1), C.byref(p)) == 1
+
+
+def test_scene_generator_deterministic(product_lib):
+    a = scenes.block((4, 3, 5), seed=11, vel_uniform=0.5, vel_sigma=0.25)
+    b = scenes.block((4, 3, 5), seed=11, vel_uniform=0.5, vel_sigma=0.25)
+    c = scenes.block((4, 3, 5), seed=12, vel_uniform=0.5, vel_sigma=0.25)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert not np.array_equal(a[0], c[0])
+    x, v = a
+    # id order: x outermost, then z, then y (src/Simulation.cpp:214-229)
+    lat = x[:, :3].reshape(4, 5, 3, 3)
+    assert np.all(np.abs(lat[1, 0, 0] - lat[0, 0, 0] - [0.5, 0, 0]) < 0.021)
+    assert np.all(np.abs(lat[0, 1, 0] - lat[0, 0, 0] - [0, 0, 0.5]) < 0.021)
+    assert np.all(np.abs(lat[0, 0, 1] - lat[0, 0, 0] - [0, 0.5, 0]) < 0.021)
+    assert np.all(x[:, 3] == 0) and np.all(v[:, 3] == 0)
+
+
+def test_scene_jitter_bounds(product_lib):
+    x, v = scenes.block((8, 8, 8), seed=3)
+    # loop order (i over x, k over z, j over y); coordinates (i, j, k)
+    gi, gk, gj = np.meshgrid(np.arange(8), np.arange(8), np.arange(8), indexing="ij")
+    ideal = 0.25 + 0.5 * np.stack([gi, gj, gk], -1).reshape(-1, 3)
+    d = x[:, :3] - ideal.astype(np.float32)
+    assert np.max(np.abs(d)) <= 0.01 + 1e-6
+    assert np.all(v == 0)
+
+
+@pytest.mark.skipif(HAS_GPU, reason="checks the no-device path")
+def test_create_without_device_fails_cleanly(product_lib):
+    p = scenes.dam_params((16, 16, 16), 2)
+    h = C.c_void_p()
+    st = product_lib.pbf_create(C.byref(p), 100, C.byref(h))
+    assert st == _capi.PBF_ERR_NO_DEVICE
+    assert b"device" in product_lib.pbf_last_error(None)
+
+
+def test_invalid_arguments_rejected_before_device(product_lib):
+    h = C.c_void_p()
+    assert product_lib.pbf_create(None, 10, C.byref(h)) == _capi.PBF_ERR_INVALID_ARGUMENT
+    p = scenes.dam_params((16, 16, 16), 2)
+    p.h = -1.0
+    assert product_lib.pbf_create(C.byref(p), 10, C.byref(h)) == _capi.PBF_ERR_INVALID_ARGUMENT
+    p = scenes.dam_params((16, 16, 16), 2)
+    assert product_lib.pbf_create(C.byref(p), 0, C.byref(h)) == _capi.PBF_ERR_INVALID_ARGUMENT
+    p.wall_lo[0] = 20.0
+    assert product_lib.pbf_create(C.byref(p), 10, C.byref(h)) == _capi.PBF_ERR_INVALID_ARGUMENT
+    assert product_lib.pbf_radix_sort(None, None, None, 5, 8, None) == _capi.PBF_ERR_INVALID_ARGUMENT
