@@ -1,0 +1,366 @@
+#!/usr/bin/env python
+"""Benchmark of the PBF substep path: particle-solver-iterations per second
+on the 2,097,152-particle dam break (128^3 lattice, spacing 0.5h, in a
+256x128x256 box, 4 solver iterations, dt = 0.008) on one GB300.
+
+A "step" is one substep (SPH::Run) over all particles.  The timed window is
+substeps 1..K of the run (default K = 50): with the workload's constants
+(epsilon = 0.01, the reference's unclamped density constraint) the dam break
+blows up after about 60 substeps and collapses into clumps of thousands of
+particles per cell, a different and degenerate workload; `stable_500`
+reports the same scene with the reference's default CFM epsilon (5) over
+the full 500 substeps.  Timed regions:
+  value    K substeps replayed from the captured CUDA graph, inputs resident
+           in HBM, bracketed by CUDA events on the simulation's stream;
+  e2e      K steps through the public C ABI with host buffers: every step
+           uploads the state from pinned host memory (pbf_set_state), runs
+           one substep (pbf_step) and reads the state back (pbf_get_state);
+  kernels  the same K substeps replayed eagerly with CUDA events around
+           every kernel, for the per-launch durations behind `roofline`.
+Each timed run starts from the initial scene, after W warm-up substeps.
+The per-substep working set (~0.5 GB) is larger than L2, so L2 is not
+flushed between steps.
+
+--impl reference times the reference path on the host cores instead: the
+oracle (a C++ restatement of pbf's GLSL compute shaders, OpenMP; the
+reference itself needs an OpenGL 4.3 context, which these machines lack).
+Each of its steps is a bounded sample of one substep: predict, sort and
+cell ranges over all particles plus the neighbour stages over a slice of
+the sorted particles, extrapolated to the full substep.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-solver-iterations/s"
+UNIT = "particle-iters/s"
+# Compulsory HBM bytes per particle of one launch (x* 16 B + lambda 4 B read
+# or written once each): lambda reads x*, writes lambda; delta-p reads x* and
+# lambda, writes x*.
+ALG_BYTES = {"lambda": 20, "delta_p": 36}
+
+
+def parse():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--scene", default="plain_2m")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-substeps", type=int, default=20,
+                    help="full substeps of the CPU baseline sample")
+    ap.add_argument("--e2e-steps", type=int, default=0, help="0: min(steps, 50)")
+    ap.add_argument("--no-stable", action="store_true", help="skip the epsilon = 5 full run")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+        self.gpu = gpu_index
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sms, maxs, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sms.append(float(parts[1]))
+                maxs.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sms:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sms.sort()
+        return {"sm_mhz": sms[len(sms) // 2], "sm_max_mhz": max(maxs), "samples": len(sms),
+                "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per particle of the dominant kernels from the committed ncu
+    summary (profiles/ncu_traffic.json), or None."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+def cpu_baseline(scene, substeps: int):
+    """FP32 oracle on all host threads, `substeps` full substeps of the scene."""
+    import oracle
+    o = oracle.Oracle(scene.params, scene.n)
+    o.set_state(scene.x4, scene.v4)
+    secs = o.step(substeps)
+    it = scene.params.num_solver_iterations
+    return {"value": scene.n * it * substeps / secs, "unit": UNIT, "cores": oracle.max_threads(),
+            "kind": "port",
+            "sample": f"{substeps} full substeps of the {scene.n}-particle dam break from its "
+                      f"initial state ({secs:.1f} s, FP32 oracle, OpenMP)"}
+
+
+def reference_arm(args, scene):
+    """The reference path's CPU implementation (the oracle port) on the host."""
+    import oracle
+    threads = oracle.max_threads()
+    o = oracle.Oracle(scene.params, scene.n)
+    o.set_state(scene.x4, scene.v4)
+    total_steps = args.steps + args.warmup
+    # slice so that the whole run takes about two minutes
+    probe_tot, probe_full, probe_slice = o.sample_substep(0, max(1, scene.n // 256))
+    per_particle = probe_slice / max(1, scene.n // 256)
+    budget = max(0.05, 120.0 / total_steps - probe_full)
+    width = int(min(scene.n, max(1024, budget / max(per_particle, 1e-12))))
+    nslices = max(1, scene.n // width)
+    est = []
+    t0 = time.perf_counter()
+    for k in range(total_steps):
+        lo = (k % nslices) * width
+        tot, _, _ = o.sample_substep(lo, min(scene.n, lo + width))
+        if k >= args.warmup:
+            est.append(tot)
+    wall = time.perf_counter() - t0
+    it = scene.params.num_solver_iterations
+    sec_per_step = sum(est) / len(est)
+    value = scene.n * it / sec_per_step
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sec_per_step * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": scene.name, "particles": scene.n, "solver_iterations": it,
+                   "lattice": scene.meta.get("lattice"), "box": scene.meta.get("box"),
+                   "sample_particles_per_step": width},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"each step: predict+sort+cells of all {scene.n} particles, "
+                                   f"solver+commit+vorticity of a {width}-particle sorted slice, "
+                                   f"extrapolated; {wall:.0f} s wall"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference = FP32 C++ restatement of pbf's GLSL shaders (the GL path needs an "
+                "OpenGL 4.3 context: unavailable on this box)",
+    }
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    from pbf_gb300 import scenes
+    scene = getattr(scenes, args.scene)()
+
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(reference_arm(args, scene)), flush=True)
+        return 0
+
+    import torch
+    import torch.distributed as dist
+    import pbf_gb300 as pg
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    K, W = args.steps, max(3, args.warmup)
+    it = scene.params.num_solver_iterations
+    stream = torch.cuda.Stream()
+    sim = pg.SPH(scene.n, tuple(scene.params.grid), scene.params)
+    sim.set_stream(stream.cuda_stream)
+
+    # warm-up (captures the graph), then reset to the initial scene
+    sim.set_state(scene.x4, scene.v4)
+    sim.step(W)
+    sim.synchronize()
+    sim.set_state(scene.x4, scene.v4)
+
+    clocks = ClockSampler(local) if rank == 0 else None
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    sim.step(K)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    sim.synchronize()  # surfaces any device status error
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop() if clocks else None
+    t = torch.tensor([ms], device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    launches = sim.kernels_per_substep() * K
+    value = world * scene.n * it * K / (ms * 1e-3)
+
+    # per-kernel durations (eager, events per kernel) over the first
+    # min(K, 50) substeps of the same window
+    KT = min(K, 50)
+    sim.set_state(scene.x4, scene.v4)
+    sim.EnableTiming(True)
+    sim.step(KT)
+    stages, counted = sim.stage_times()
+    sim.EnableTiming(False)
+    # k_delta_p is the top kernel of the ncu launch list (the lambda stage is
+    # split over two kernels, k_lambda_build and k_lambda)
+    per_launch = {"lambda": stages["lambda"] / (counted * it),
+                  "delta_p": stages["delta_p"] / (counted * it)}
+    dom = "delta_p"
+    peak, peak_kind = measured_peaks()
+    achieved = ALG_BYTES[dom] * scene.n / (per_launch[dom] * 1e-3) / 1e9
+    prof = profiled_traffic()
+    traffic = None
+    if prof and dom in prof.get("bytes_per_particle", {}):
+        traffic = prof["bytes_per_particle"][dom] * scene.n
+    total_stage = sum(stages.values())
+
+    # end to end through the C ABI with pinned host buffers
+    E = args.e2e_steps or min(K, 50)
+    hx = [torch.from_numpy(scene.x4.copy()).pin_memory() for _ in range(2)]
+    hv = [torch.from_numpy(scene.v4.copy()).pin_memory() for _ in range(2)]
+    lib = pg.load()
+    h = sim.handle
+    barrier()
+    torch.cuda.synchronize()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for k in range(E):
+        a, b = k % 2, (k + 1) % 2
+        pg._capi.check(lib.pbf_set_state(h, hx[a].data_ptr(), hv[a].data_ptr(), pg.PBF_HOST), h)
+        pg._capi.check(lib.pbf_step(h, 1), h)
+        pg._capi.check(lib.pbf_get_state(h, hx[b].data_ptr(), hv[b].data_ptr(), pg.PBF_HOST), h)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = f0.elapsed_time(f1)
+    t = torch.tensor([e2e_ms], device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    e2e_ms = float(t.item())
+    e2e_value = world * scene.n * it * E / (e2e_ms * 1e-3)
+
+    # the same scene with the reference's default epsilon: a stable run of
+    # the full 500 substeps
+    stable = None
+    if not args.no_stable:
+        ps = scene.params.copy()
+        ps.epsilon = 5.0
+        sim.set_params(ps)
+        sim.set_state(scene.x4, scene.v4)
+        sim.step(3)
+        sim.set_state(scene.x4, scene.v4)
+        torch.cuda.synchronize()
+        g0 = torch.cuda.Event(enable_timing=True)
+        g1 = torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        sim.step(scene.substeps)
+        g1.record(stream)
+        torch.cuda.synchronize()
+        sim.synchronize()
+        sms = g0.elapsed_time(g1)
+        stable = {"value": scene.n * it * scene.substeps / (sms * 1e-3), "unit": UNIT,
+                  "substeps": scene.substeps, "ms_per_step": sms / scene.substeps,
+                  "epsilon": 5.0, "note": "same scene and constants except CFM epsilon = 5 "
+                                          "(src/SPH.cpp:138), full run"}
+        sim.set_params(scene.params)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(scene, args.cpu_substeps)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+            "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": scene.name, "particles": scene.n, "solver_iterations": it,
+                       "lattice": scene.meta.get("lattice"), "box": scene.meta.get("box"),
+                       "grid": list(scene.params.grid), "dt": scene.params.timestep,
+                       "substeps_timed": K, "window": f"substeps 1-{K} of {scene.substeps}",
+                       "l2": "working set > L2 (no flush)",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "e2e": {"value": e2e_value, "unit": UNIT,
+                    "h2d_bytes_per_step": 2 * 16 * scene.n, "d2h_bytes_per_step": 2 * 16 * scene.n,
+                    "ms_per_step": e2e_ms / E, "steps": E},
+            "roofline": {"bound": "hbm", "kernel": "k_delta_p", "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "alg_bytes_per_launch": ALG_BYTES[dom] * scene.n,
+                         "ms_per_launch": per_launch[dom],
+                         "note": "neighbour sweeps are FP32-issue / L1-gather bound, not HBM"},
+            "kernel_ms_per_substep": {k: v / counted for k, v in stages.items()},
+            "kernel_share": {k: v / total_stage for k, v in stages.items()},
+            "gpu_launches": launches,
+            "stable_500": stable,
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -18,8 +18,9 @@
  *    buffers (src/SPH.h:49,181; shaders/sph/update.glsl:26-27).  The w lane is
  *    written as 0 and ignored on input.
  *  - A handle is bound to the CUDA device that was current at creation and
- *    to one CUDA stream (default: the legacy default stream).  Calls on one
- *    handle are not thread-safe, matching the reference's single GL context.
+ *    to one CUDA stream (default: a non-blocking stream the handle owns).
+ *    Calls on one handle are not thread-safe, matching the reference's
+ *    single GL context.
  *  - Stepping is asynchronous.  Device-side failures (non-finite positions, a
  *    sort lookback that ran out of its spin budget) are latched in a device
  *    status word and reported by the next synchronising call (pbf_synchronize,
@@ -127,8 +128,9 @@ pbf_status pbf_set_params(pbf_sim* sim, const pbf_params* params);
 pbf_status pbf_get_params(const pbf_sim* sim, pbf_params* out);
 uint32_t pbf_num_particles(const pbf_sim* sim);
 
-/* Binds the handle to a CUDA stream (cudaStream_t passed as void*); NULL is
- * the legacy default stream. */
+/* Binds the handle to a CUDA stream (cudaStream_t passed as void*); NULL
+ * restores the handle's own stream.  The substep is captured as a CUDA graph,
+ * so the legacy default stream cannot be used. */
 pbf_status pbf_set_stream(pbf_sim* sim, void* stream);
 
 /* Initial particle state, float4 per particle in id order; what the
@@ -154,16 +156,45 @@ pbf_status pbf_device_buffers(pbf_sim* sim, float** x4, float** v4);
  * replayed from a captured CUDA graph. */
 pbf_status pbf_step(pbf_sim* sim, uint32_t substeps);
 
+/* Performance knobs of a handle.  None of them changes any result: every
+ * setting produces the same bits (the tests check this). */
+typedef struct pbf_tuning {
+    uint32_t use_neighbour_lists; /* 1: the first lambda sweep of a substep records each
+                                     particle's candidates within h + skin (in the
+                                     reference's visit order) and later sweeps replay
+                                     them while a displacement guard proves no other
+                                     candidate can be within h; 0: every sweep scans the
+                                     full 27-cell stencil (the reference's loop) */
+    uint32_t list_capacity;       /* entries per particle; longer lists fall back to the
+                                     full stencil scan for that particle */
+    float skin_h;                 /* list radius is h * (1 + skin_h) */
+} pbf_tuning;
+
+/* No reference counterpart (the reference has no tuning surface). */
+pbf_status pbf_set_tuning(pbf_sim* sim, const pbf_tuning* tuning);
+pbf_status pbf_get_tuning(const pbf_sim* sim, pbf_tuning* out);
+
 /* Waits for the handle's stream and reports the device status word. */
 pbf_status pbf_synchronize(pbf_sim* sim);
 pbf_status pbf_device_status(pbf_sim* sim, uint32_t* bits);
 
 /* Per-phase timers, the counterpart of SPH's GL_TIME_ELAPSED queries
  * (src/SPH.cpp:218-240): predict, sort, neighbour cells, solver,
- * commit + vorticity.  When enabled, pbf_step runs the stages eagerly with
- * CUDA events between them; ms[5] receives the last substep's times. */
+ * commit + vorticity.  When enabled, pbf_step runs each substep eagerly
+ * with CUDA events between the stages and waits for it; ms[5] receives the
+ * last substep's times.  Enabling (or re-enabling) resets the sums below. */
 pbf_status pbf_enable_timing(pbf_sim* sim, int enable);
 pbf_status pbf_get_timing(pbf_sim* sim, float ms[5]);
+
+/* Stage sums (ms) over all substeps run since timing was last enabled:
+ * predict, sort, cell ranges, lambda (all iterations), delta-p (all
+ * iterations), commit, XSPH/vorticity pass A, vorticity pass B.  *substeps
+ * receives how many substeps the sums cover.  No reference counterpart; the
+ * per-kernel split of the phases above. */
+pbf_status pbf_get_stage_times(pbf_sim* sim, double ms_sum[8], uint32_t* substeps);
+
+/* Number of kernels one substep launches (for launch accounting). */
+uint32_t pbf_kernels_per_substep(const pbf_sim* sim);
 
 /* ---- debug reads of the last substep's intermediates (synchronising) -------- */
 

@@ -70,6 +70,8 @@ def load() -> C.CDLL:
         lib.pbfo_diagnostics.argtypes = [P, P]
         lib.pbfo_radix_sort.argtypes = [P, C.c_uint32, C.c_uint32, P, P]
         lib.pbfo_max_threads.restype = C.c_int
+        lib.pbfo_sample_substep.restype = C.c_double
+        lib.pbfo_sample_substep.argtypes = [P, C.c_uint32, C.c_uint32, P, P]
         _lib = lib
     return _lib
 
@@ -149,6 +151,14 @@ class Oracle:
         out = np.empty(4, np.float64)
         self._lib.pbfo_get_consts(self._h, out.ctypes.data)
         return {"k6": out[0], "kg": out[1], "kg_lambda": out[2], "h2": out[3]}
+
+    def sample_substep(self, lo: int, hi: int):
+        """Timing sample: (extrapolated s per substep, s of all-particle stages, s of slice)."""
+        tf = C.c_double()
+        ts = C.c_double()
+        tot = self._lib.pbfo_sample_substep(self._h, int(lo), int(hi), C.addressof(tf),
+                                            C.addressof(ts))
+        return float(tot), tf.value, ts.value
 
     def diagnostics(self):
         out = np.empty(4, np.float64)

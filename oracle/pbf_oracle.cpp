@@ -187,6 +187,20 @@ void pbfo_radix_sort(const uint32_t* keys, uint32_t n, uint32_t numbits, uint32_
     }
 }
 
+// Timing sample (see Sim::sample_substep): returns the extrapolated seconds
+// of one full substep, t_full + t_slice * n / (hi - lo).
+double pbfo_sample_substep(void* hp, uint32_t lo, uint32_t hi, double* t_full, double* t_slice) {
+    Handle* h = (Handle*)hp;
+    const uint32_t n = h->fp64 ? h->d.n : h->f.n;
+    if (hi > n) hi = n;
+    if (lo >= hi) return 0.0;
+    if (h->fp64)
+        h->d.sample_substep(lo, hi, t_full, t_slice);
+    else
+        h->f.sample_substep(lo, hi, t_full, t_slice);
+    return *t_full + *t_slice * (double)n / (double)(hi - lo);
+}
+
 int pbfo_max_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();

@@ -41,6 +41,7 @@
 #pragma once
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -388,11 +389,12 @@ struct Sim {
                 if ((uint32_t)j != i) f((uint32_t)j);
     }
 
-    // calclambda.glsl:66-102, reading positions `P`.
-    void calc_lambda(const std::vector<V3<T>>& P) {
+    // calclambda.glsl:66-102, reading positions `P`, for sorted [lo, hi).
+    void calc_lambda(const std::vector<V3<T>>& P, int64_t lo = 0, int64_t hi = -1) {
         const int nt = threads();
+        if (hi < 0) hi = n;
 #pragma omp parallel for schedule(dynamic, 256) num_threads(nt)
-        for (int64_t ii = 0; ii < (int64_t)n; ++ii) {
+        for (int64_t ii = lo; ii < hi; ++ii) {
             const uint32_t i = (uint32_t)ii;
             const V3<T> pi = P[i];
             T rho = 0, sumk = 0;
@@ -413,11 +415,13 @@ struct Sim {
         }
     }
 
-    // updatepos.glsl:42-104, reading `P` and lambda, writing `Q`.
-    void update_pos(const std::vector<V3<T>>& P, std::vector<V3<T>>& Q) {
+    // updatepos.glsl:42-104, reading `P` and lambda, writing `Q`, for sorted [lo, hi).
+    void update_pos(const std::vector<V3<T>>& P, std::vector<V3<T>>& Q, int64_t lo = 0,
+                    int64_t hi = -1) {
         const int nt = threads();
+        if (hi < 0) hi = n;
 #pragma omp parallel for schedule(dynamic, 256) num_threads(nt)
-        for (int64_t ii = 0; ii < (int64_t)n; ++ii) {
+        for (int64_t ii = lo; ii < hi; ++ii) {
             const uint32_t i = (uint32_t)ii;
             const V3<T> pi = P[i];
             const T li = lambda[i];
@@ -444,10 +448,11 @@ struct Sim {
     }
 
     // update.glsl:16-28: velocity from the displacement, back to id order.
-    void commit(const std::vector<V3<T>>& P) {
+    void commit(const std::vector<V3<T>>& P, int64_t lo = 0, int64_t hi = -1) {
         const int nt = threads();
+        if (hi < 0) hi = n;
 #pragma omp parallel for schedule(static) num_threads(nt)
-        for (int64_t ii = 0; ii < (int64_t)n; ++ii) {
+        for (int64_t ii = lo; ii < hi; ++ii) {
             const uint32_t id = perm[ii];
             const V3<T> q = P[ii];
             const V3<T> xo = x[id];
@@ -458,10 +463,11 @@ struct Sim {
 
     // vorticity.glsl:34-60 (pass A, XSPH + vorticity vector) and :65-85
     // (pass B, confinement), Jacobi between and within the passes.
-    void vorticity(const std::vector<V3<T>>& P) {
+    void vorticity(const std::vector<V3<T>>& P, int64_t lo = 0, int64_t hi = -1) {
         const int nt = threads();
+        if (hi < 0) hi = n;
 #pragma omp parallel for schedule(dynamic, 256) num_threads(nt)
-        for (int64_t ii = 0; ii < (int64_t)n; ++ii) {
+        for (int64_t ii = lo; ii < hi; ++ii) {
             const uint32_t i = (uint32_t)ii;
             const V3<T> pi = P[i];
             const V3<T> vi = vs[i];
@@ -482,7 +488,7 @@ struct Sim {
             omag[i] = std::sqrt(dot3(w, w));     // :60
         }
 #pragma omp parallel for schedule(dynamic, 256) num_threads(nt)
-        for (int64_t ii = 0; ii < (int64_t)n; ++ii) {
+        for (int64_t ii = lo; ii < hi; ++ii) {
             const uint32_t i = (uint32_t)ii;
             const V3<T> pi = P[i];
             V3<T> eta{0, 0, 0};
@@ -536,6 +542,31 @@ struct Sim {
             for (int64_t ii = 0; ii < (int64_t)n; ++ii) v[perm[ii]] = vs[ii];
         }
         if (cur != &pa) pa = *cur;  // pa holds the final sorted positions
+    }
+
+    // A bounded timing sample of one substep: predict, sort and cell ranges
+    // over all n particles, then the solver, commit and vorticity stages over
+    // the sorted slice [lo, hi) only.  Returns the seconds of the two parts.
+    // For timing only: particles outside the slice keep stale solver data.
+    void sample_substep(int64_t lo, int64_t hi, double* t_full, double* t_slice) {
+        auto t0 = std::chrono::steady_clock::now();
+        predict();
+        sort();
+        find_cells();
+        auto t1 = std::chrono::steady_clock::now();
+        std::copy(xpred.begin() + lo, xpred.begin() + hi, pa.begin() + lo);
+        std::vector<V3<T>>* cur = &pa;
+        std::vector<V3<T>>* nxt = &pb;
+        for (uint32_t it = 0; it < p.num_solver_iterations; ++it) {
+            calc_lambda(*cur, lo, hi);
+            update_pos(*cur, *nxt, lo, hi);
+            std::swap(cur, nxt);
+        }
+        commit(*cur, lo, hi);
+        if (p.vorticity_confinement) vorticity(*cur, lo, hi);
+        auto t2 = std::chrono::steady_clock::now();
+        *t_full = std::chrono::duration<double>(t1 - t0).count();
+        *t_slice = std::chrono::duration<double>(t2 - t1).count();
     }
 
     // Density error and kinetic energy of the current state, with a fresh

@@ -61,6 +61,16 @@ class Params(C.Structure):
         return d
 
 
+class Tuning(C.Structure):
+    """pbf_tuning (include/pbf.h)."""
+
+    _fields_ = [
+        ("use_neighbour_lists", C.c_uint32),
+        ("list_capacity", C.c_uint32),
+        ("skin_h", C.c_float),
+    ]
+
+
 class Diagnostics(C.Structure):
     _fields_ = [
         ("mean_density_error", C.c_double),
@@ -92,9 +102,13 @@ SIGNATURES = {
     "pbf_device_buffers": (C.c_int, [_P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
     "pbf_step": (C.c_int, [_P, C.c_uint32]),
     "pbf_synchronize": (C.c_int, [_P]),
+    "pbf_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+    "pbf_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
     "pbf_device_status": (C.c_int, [_P, _U32P]),
     "pbf_enable_timing": (C.c_int, [_P, C.c_int]),
     "pbf_get_timing": (C.c_int, [_P, _F]),
+    "pbf_get_stage_times": (C.c_int, [_P, C.POINTER(C.c_double), _U32P]),
+    "pbf_kernels_per_substep": (C.c_uint32, [_P]),
     "pbf_get_sort": (C.c_int, [_P, _P, _P, _P]),
     "pbf_get_cells": (C.c_int, [_P, _P, _P]),
     "pbf_get_solver": (C.c_int, [_P, _P, _P]),

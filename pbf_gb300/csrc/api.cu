@@ -42,6 +42,13 @@ struct pbf_sim {
     uint32_t *keys = nullptr, *skeys = nullptr, *perm = nullptr;
     int32_t *cstart = nullptr, *cend = nullptr;
     uint32_t* status = nullptr;  // device status word [0], bad-key flag [1]
+    // neighbour lists (pbf_tuning)
+    pbf_tuning tuning{};
+    uint32_t* nbr_idx = nullptr;
+    int32_t* nbr_cnt = nullptr;
+    uint32_t* guard = nullptr;
+    uint32_t nbr_cap = 0;       // capacity of nbr_idx in entries per particle
+    uint32_t guard_slots = 0;
     uint32_t* h_status = nullptr;
     void* sort_mem = nullptr;
     SortWorkspace sort;
@@ -51,8 +58,10 @@ struct pbf_sim {
     bool graph_valid = false;
 
     bool timing = false;
-    cudaEvent_t ev[6] = {};
-    float ms[5] = {};
+    std::vector<cudaEvent_t> ev;  // 7 + 2 * iterations stage boundaries
+    float ms[5] = {};             // reference phases of the last timed substep
+    double stage_ms[8] = {};      // stage sums since timing was enabled
+    uint32_t timed_substeps = 0;
 
     std::string err;
 };
@@ -160,9 +169,55 @@ DevConsts make_consts(const pbf_params& p) {
     return c;
 }
 
+void apply_tuning(DevConsts& c, const pbf_params& p, const pbf_tuning& t) {
+    c.use_lists = t.use_neighbour_lists ? 1u : 0u;
+    c.skin = t.skin_h * p.h;
+    const double rl = (double)p.h + (double)c.skin;
+    c.r2list = (float)(rl * rl * (1.0 + 1e-5));
+    c.margin_h = 1e-3f * p.h;
+    float wm = 0.0f;
+    for (int a = 0; a < 3; ++a) wm = std::fmax(wm, std::fmax(std::fabs(p.wall_lo[a]), std::fabs(p.wall_hi[a])));
+    c.wall_abs_max = wm;
+}
+
+pbf_tuning default_tuning() {
+    pbf_tuning t{};
+    t.use_neighbour_lists = 1;
+    t.list_capacity = 128;
+    t.skin_h = 0.15f;
+    return t;
+}
+
 template <typename T>
 cudaError_t dalloc(T** p, size_t count) {
     return cudaMalloc((void**)p, sizeof(T) * (count > 0 ? count : 1));
+}
+
+// (Re)allocates the neighbour-list and guard buffers for the current
+// tuning and iteration count.
+cudaError_t ensure_lists(pbf_sim* s) {
+    const uint32_t cap = s->tuning.use_neighbour_lists ? s->tuning.list_capacity : 0u;
+    if (cap != s->nbr_cap || !s->nbr_cnt) {
+        if (s->nbr_idx) cudaFree(s->nbr_idx);
+        if (s->nbr_cnt) cudaFree(s->nbr_cnt);
+        s->nbr_idx = nullptr;
+        s->nbr_cnt = nullptr;
+        s->nbr_cap = 0;
+        cudaError_t e = dalloc(&s->nbr_idx, (size_t)(cap > 0 ? cap : 1) * s->n);
+        if (e == cudaSuccess) e = dalloc(&s->nbr_cnt, s->n);
+        if (e != cudaSuccess) return e;
+        s->nbr_cap = cap;
+    }
+    const uint32_t slots = 2 + s->params.num_solver_iterations;
+    if (slots > s->guard_slots) {
+        if (s->guard) cudaFree(s->guard);
+        s->guard = nullptr;
+        s->guard_slots = 0;
+        cudaError_t e = dalloc(&s->guard, slots);
+        if (e != cudaSuccess) return e;
+        s->guard_slots = slots;
+    }
+    return cudaSuccess;
 }
 
 void free_sim(pbf_sim* s) {
@@ -175,12 +230,14 @@ void free_sim(pbf_sim* s) {
     if (s->graph) cudaGraphDestroy(s->graph);
     void* bufs[] = {s->x,  s->v,  s->xstar, s->XP,   s->Pa,     s->Pb,   s->L,
                     s->VS, s->VX, s->OM,    s->Q,    s->keys,   s->skeys, s->perm,
-                    s->cstart, s->cend, s->status, s->sort_mem};
+                    s->cstart, s->cend, s->status, s->sort_mem, s->nbr_idx, s->nbr_cnt,
+                    s->guard};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (s->h_status) cudaFreeHost(s->h_status);
     for (cudaEvent_t e : s->ev)
         if (e) cudaEventDestroy(e);
+    s->ev.clear();
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     cudaSetDevice(prev);
     delete s;
@@ -198,54 +255,83 @@ struct DeviceGuard {
     }
 };
 
-// Final sorted positions of a substep with `iters` solver iterations.
-float4* final_positions(pbf_sim* s, uint32_t iters) {
-    if (iters == 0) return s->XP;
-    return (iters % 2 == 1) ? s->Pa : s->Pb;
+// Kernel launches per substep (the sort's launches plus one per stage).
+uint32_t kernels_per_substep(const pbf_sim* s) {
+    const uint32_t passes = (s->numbits + 7) / 8;
+    return 1u /*predict*/ + 1u /*unmark*/ + 2u + passes /*sort*/ + 1u /*cells*/ +
+           2u * s->params.num_solver_iterations + 1u /*commit*/ +
+           (s->params.vorticity_confinement ? 2u : 0u);
 }
 
 // Enqueues one substep (SPH::Run, src/SPH.cpp:246-334) on s->stream.  With
-// `ev` non-null, records an event after each of the five reference phases.
+// `ev` non-null, records an event at every stage boundary: before predict,
+// after predict, sort, cells, each lambda and delta-p launch, commit and the
+// two vorticity passes (7 + 2 * iterations events).
 cudaError_t enqueue_substep(pbf_sim* s, cudaEvent_t* ev) {
     const uint32_t n = s->n;
+    if (!s->nbr_cnt || s->guard_slots < 2 + s->params.num_solver_iterations)
+        return cudaErrorInvalidValue;  // ensure_lists() runs before any capture
     const unsigned g = grid_for(n);
     const DevConsts& c = s->dc;
+    const uint32_t iters = s->params.num_solver_iterations;
     cudaStream_t st = s->stream;
-    if (ev) cudaEventRecord(ev[0], st);
+    auto mark = [&](uint32_t idx) {
+        if (ev) cudaEventRecord(ev[idx], st);
+    };
+    mark(0);
     // 1 predict (predictpos.glsl)
     k_predict<<<g, kBlock, 0, st>>>(s->x, s->v, s->xstar, s->keys, n, c, s->status);
-    if (ev) cudaEventRecord(ev[1], st);
+    mark(1);
     // 2 sort (RadixSort::Run); first clear the cell starts of the previous
     // substep while its sorted keys are still there
     k_unmark_cells<<<g, kBlock, 0, st>>>(s->skeys, n, s->ncells, s->cstart);
     cudaError_t e = sort_pairs(s->sort, s->keys, s->skeys, s->perm, n, s->numbits, s->status, st);
     if (e != cudaSuccess) return e;
-    if (ev) cudaEventRecord(ev[2], st);
+    mark(2);
     // 3 cell ranges (NeighbourCellFinder::FindNeighbourCells)
     k_find_cells<<<g, kBlock, 0, st>>>(s->skeys, s->perm, s->xstar, s->XP, n, s->ncells, s->cstart,
                                        s->cend, s->status + 1);
-    if (ev) cudaEventRecord(ev[3], st);
-    // 4 solver iterations (calclambda / updatepos)
+    mark(3);
+    // 4 solver iterations (calclambda / updatepos).  The first lambda sweep
+    // also records the neighbour lists the later sweeps replay.
+    const NbrLists nl{s->nbr_idx, s->nbr_cnt, s->guard, s->nbr_cap, n};
+    DevConsts cv = c;  // without iterations no list is built this substep
+    if (iters == 0) cv.use_lists = 0;
+    cudaError_t ge = cudaMemsetAsync(s->guard, 0, sizeof(uint32_t) * (2 + iters), st);
+    if (ge != cudaSuccess) return ge;
     const float4* cur = s->XP;
-    for (uint32_t it = 0; it < s->params.num_solver_iterations; ++it) {
+    for (uint32_t it = 0; it < iters; ++it) {
         float4* nxt = (it % 2 == 0) ? s->Pa : s->Pb;
-        k_lambda<<<g, kBlock, 0, st>>>(cur, s->skeys, s->cstart, s->cend, s->L, n, c);
-        k_delta_p<<<g, kBlock, 0, st>>>(s->L, s->skeys, s->cstart, s->cend, nxt, n, c, s->status);
+        const int in_slot = it == 0 ? -1 : (int)it;  // displacement of `cur` from XP
+        if (it == 0)
+            k_lambda_build<<<g, kBlock, 0, st>>>(s->XP, s->skeys, s->cstart, s->cend, s->L, nl, n, c);
+        else
+            k_lambda<<<g, kBlock, 0, st>>>(cur, s->XP, s->skeys, s->cstart, s->cend, s->L, nl,
+                                           in_slot, n, c);
+        mark(4 + 2 * it);
+        k_delta_p<<<g, kBlock, 0, st>>>(s->L, s->XP, s->skeys, s->cstart, s->cend, nxt, nl, in_slot,
+                                        (int)it + 1, n, c, s->status);
+        mark(5 + 2 * it);
         cur = nxt;
     }
-    if (ev) cudaEventRecord(ev[4], st);
     // 5 commit (update.glsl) and XSPH + vorticity (vorticity.glsl)
     const bool vort = s->params.vorticity_confinement != 0;
+    const int fin_slot = iters == 0 ? -1 : (int)iters;
     k_commit<<<g, kBlock, 0, st>>>(cur, s->perm, s->x, s->VS, vort ? nullptr : s->v, n, c);
-    if (vort) {
-        k_vorticity_a<<<g, kBlock, 0, st>>>(cur, s->VS, s->skeys, s->cstart, s->cend, s->VX, s->OM,
-                                            s->Q, n, c);
-        k_vorticity_b<<<g, kBlock, 0, st>>>(s->Q, s->VX, s->OM, s->skeys, s->perm, s->cstart,
-                                            s->cend, s->v, n, c);
-    }
-    if (ev) cudaEventRecord(ev[5], st);
+    mark(4 + 2 * iters);
+    if (vort)
+        k_vorticity_a<<<g, kBlock, 0, st>>>(cur, s->XP, s->VS, s->skeys, s->cstart, s->cend, s->VX,
+                                            s->OM, s->Q, nl, fin_slot, n, cv);
+    mark(5 + 2 * iters);
+    if (vort)
+        k_vorticity_b<<<g, kBlock, 0, st>>>(s->Q, s->XP, s->VX, s->OM, s->skeys, s->perm, s->cstart,
+                                            s->cend, s->v, nl, fin_slot, n, cv);
+    mark(6 + 2 * iters);
     return cudaGetLastError();
 }
+
+// One eager substep with stage events; accumulates the stage sums.
+pbf_status timed_substep(pbf_sim* s);
 
 void invalidate_graph(pbf_sim* s) {
     if (s->exec) cudaGraphExecDestroy(s->exec);
@@ -270,6 +356,40 @@ pbf_status check_status(pbf_sim* s) {
     return PBF_OK;
 }
 
+pbf_status timed_substep(pbf_sim* s) {
+    const uint32_t iters = s->params.num_solver_iterations;
+    const size_t need = 7 + 2 * (size_t)iters;
+    while (s->ev.size() < need) {
+        cudaEvent_t e = nullptr;
+        PBF_CUDA(s, cudaEventCreate(&e));
+        s->ev.push_back(e);
+    }
+    cudaError_t e = enqueue_substep(s, s->ev.data());
+    if (e != cudaSuccess) return cuda_fail(s, e, "substep launch");
+    PBF_CUDA(s, cudaEventSynchronize(s->ev[need - 1]));
+    auto span = [&](size_t a, size_t b) {
+        float m = 0.0f;
+        cudaEventElapsedTime(&m, s->ev[a], s->ev[b]);
+        return (double)m;
+    };
+    double lam = 0.0, dp = 0.0;
+    for (uint32_t it = 0; it < iters; ++it) {
+        lam += span(3 + 2 * it, 4 + 2 * it);
+        dp += span(4 + 2 * it, 5 + 2 * it);
+    }
+    const double st[8] = {span(0, 1), span(1, 2), span(2, 3), lam, dp,
+                          span(3 + 2 * iters, 4 + 2 * iters), span(4 + 2 * iters, 5 + 2 * iters),
+                          span(5 + 2 * iters, 6 + 2 * iters)};
+    for (int i = 0; i < 8; ++i) s->stage_ms[i] += st[i];
+    s->timed_substeps++;
+    s->ms[0] = (float)st[0];
+    s->ms[1] = (float)st[1];
+    s->ms[2] = (float)st[2];
+    s->ms[3] = (float)(lam + dp);
+    s->ms[4] = (float)(st[5] + st[6] + st[7]);
+    return PBF_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -288,7 +408,9 @@ pbf_status pbf_create(const pbf_params* params, uint32_t n, pbf_sim** out) {
     pbf_sim* s = new pbf_sim();
     cudaGetDevice(&s->device);
     s->params = *params;
+    s->tuning = default_tuning();
     s->dc = make_consts(*params);
+    apply_tuning(s->dc, s->params, s->tuning);
     s->n = n;
     s->ncells = params->grid[0] * params->grid[1] * params->grid[2];
     s->numbits = sort_numbits_for_cells(s->ncells);
@@ -300,9 +422,9 @@ pbf_status pbf_create(const pbf_params* params, uint32_t n, pbf_sim** out) {
     ALLOC(perm, n) ALLOC(cstart, s->ncells) ALLOC(cend, s->ncells) ALLOC(status, 2)
 #undef ALLOC
     if (e == cudaSuccess) e = cudaMalloc(&s->sort_mem, SortWorkspace::bytes_for(n));
+    if (e == cudaSuccess) e = ensure_lists(s);
     if (e == cudaSuccess) e = cudaMallocHost((void**)&s->h_status, 2 * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
-    for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&s->ev[i]);
     if (e != cudaSuccess) {
         pbf_status st = cuda_fail(nullptr, e, "pbf_create allocation");
         free_sim(s);
@@ -339,7 +461,32 @@ pbf_status pbf_set_params(pbf_sim* s, const pbf_params* p) {
             return fail(s, PBF_ERR_INVALID_ARGUMENT, "the grid is fixed at creation");
     s->params = *p;
     s->dc = make_consts(*p);
+    apply_tuning(s->dc, s->params, s->tuning);
     invalidate_graph(s);
+    DeviceGuard dg(s->device);
+    PBF_CUDA(s, cudaStreamSynchronize(s->stream));
+    PBF_CUDA(s, ensure_lists(s));
+    return PBF_OK;
+}
+
+pbf_status pbf_set_tuning(pbf_sim* s, const pbf_tuning* t) {
+    if (!s || !t) return fail(s, PBF_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (t->use_neighbour_lists && (t->list_capacity < 1 || t->list_capacity > 4096))
+        return fail(s, PBF_ERR_INVALID_ARGUMENT, "list_capacity must be in [1, 4096]");
+    if (!(t->skin_h >= 0.0f) || !(t->skin_h <= 1.0f))
+        return fail(s, PBF_ERR_INVALID_ARGUMENT, "skin_h must be in [0, 1]");
+    DeviceGuard dg(s->device);
+    PBF_CUDA(s, cudaStreamSynchronize(s->stream));
+    s->tuning = *t;
+    apply_tuning(s->dc, s->params, s->tuning);
+    invalidate_graph(s);
+    PBF_CUDA(s, ensure_lists(s));
+    return PBF_OK;
+}
+
+pbf_status pbf_get_tuning(const pbf_sim* s, pbf_tuning* out) {
+    if (!s || !out) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = s->tuning;
     return PBF_OK;
 }
 
@@ -355,7 +502,9 @@ pbf_status pbf_set_stream(pbf_sim* s, void* stream) {
     if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
     DeviceGuard dg(s->device);
     PBF_CUDA(s, cudaStreamSynchronize(s->stream));
-    s->stream = stream ? (cudaStream_t)stream : s->own_stream;
+    cudaStream_t ns = stream ? (cudaStream_t)stream : s->own_stream;
+    if (ns != s->stream) invalidate_graph(s);  // the graph is replayed on any stream, but
+    s->stream = ns;                            // re-capture keeps capture and replay alike
     return PBF_OK;
 }
 
@@ -393,12 +542,8 @@ pbf_status pbf_step(pbf_sim* s, uint32_t substeps) {
     DeviceGuard dg(s->device);
     if (s->timing) {
         for (uint32_t k = 0; k < substeps; ++k) {
-            cudaError_t e = enqueue_substep(s, s->ev);
-            if (e != cudaSuccess) return cuda_fail(s, e, "substep launch");
-        }
-        if (substeps > 0) {
-            PBF_CUDA(s, cudaEventSynchronize(s->ev[5]));
-            for (int p = 0; p < 5; ++p) cudaEventElapsedTime(&s->ms[p], s->ev[p], s->ev[p + 1]);
+            pbf_status r = timed_substep(s);
+            if (r != PBF_OK) return r;
         }
         return PBF_OK;
     }
@@ -440,8 +585,19 @@ pbf_status pbf_device_status(pbf_sim* s, uint32_t* bits) {
 pbf_status pbf_enable_timing(pbf_sim* s, int enable) {
     if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
     s->timing = enable != 0;
+    for (double& m : s->stage_ms) m = 0.0;
+    s->timed_substeps = 0;
     return PBF_OK;
 }
+
+pbf_status pbf_get_stage_times(pbf_sim* s, double ms_sum[8], uint32_t* substeps) {
+    if (!s || !ms_sum) return fail(s, PBF_ERR_INVALID_ARGUMENT, "NULL argument");
+    for (int i = 0; i < 8; ++i) ms_sum[i] = s->stage_ms[i];
+    if (substeps) *substeps = s->timed_substeps;
+    return PBF_OK;
+}
+
+uint32_t pbf_kernels_per_substep(const pbf_sim* s) { return s ? kernels_per_substep(s) : 0; }
 
 pbf_status pbf_get_timing(pbf_sim* s, float ms[5]) {
     if (!s || !ms) return fail(s, PBF_ERR_INVALID_ARGUMENT, "NULL argument");

@@ -36,6 +36,26 @@ struct DevConsts {
     uint32_t GxGz;    // hash weight of y (src/SPH.cpp:31)
     uint32_t ncells;
     uint32_t ext_force;
+    // neighbour lists (a tuning choice: results are identical with or without)
+    uint32_t use_lists;
+    float skin;          // list radius is h + skin
+    float r2list;        // inclusion threshold on |d|^2 at the predicted positions
+    float margin_h;      // fixed part of the guard's rounding margin
+    float wall_abs_max;  // largest |wall| coordinate (positions are clamped inside)
+};
+
+// Order-preserving neighbour lists of one substep.  idx is [cap][n] (entry k
+// of particle i at idx[k * n + i], coalesced across a warp); cnt[i] = -1
+// marks a particle whose list overflowed (it always scans its full stencil).
+// guard[0] holds the largest coordinate magnitude of the predicted positions,
+// guard[1 + k] the largest displacement from them after delta-p iteration k
+// (both as float bits).
+struct NbrLists {
+    uint32_t* idx;
+    int32_t* cnt;
+    uint32_t* guard;
+    uint32_t cap;
+    uint32_t n;
 };
 
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }

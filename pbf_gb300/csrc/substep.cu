@@ -117,60 +117,173 @@ k_find_cells(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ pe
     if (i + 1 == n || skeys[i + 1] != k) cend[k] = (int32_t)(i + 1);
 }
 
-// calclambda.glsl:66-102.  Reads positions P, writes L[i] = (p_i, lambda_i).
-__global__ void __launch_bounds__(kBlock)
-k_lambda(const float4* __restrict__ P, const uint32_t* __restrict__ skeys,
-         const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
-         float4* __restrict__ L, uint32_t n, DevConsts c) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+// ---- neighbour visitors ------------------------------------------------------
+//
+// Two ways to enumerate the candidates of sorted particle i, both in the
+// reference's order:
+//  full  the 9 stencil rows, each row's run in ascending index, i skipped;
+//  list  the candidates that were within h + skin at the substep's predicted
+//        positions, stored by the first lambda sweep in that same order.
+// A candidate left out of the list was farther than h + skin apart at the
+// predicted positions; while every particle has moved less than
+// (skin - margin) / 2 since (the guard below), it is still farther than h
+// apart in floating point, so it would have contributed nothing.  Both
+// visitors therefore produce the same sums, bit for bit.
+
+template <class F>
+__device__ __forceinline__ void visit_full(uint32_t i, uint32_t key, const DevConsts& c,
+                                           const int32_t* __restrict__ cstart,
+                                           const int32_t* __restrict__ cend, F&& f) {
+    // The 9 ranges live in a small local array: computing each row inside the
+    // loop instead raises register use and lowers occupancy (measured slower).
     Runs r;
-    runs_of(skeys[i], c, cstart, cend, r);
-    const float3 pi = xyz(P[i]);
-    float rho = 0.0f, sumk = 0.0f;
-    float3 gi = make_float3(0.0f, 0.0f, 0.0f);
-    for (int o = 0; o < 9; ++o) {
-        for (int32_t j = r.b[o]; j < r.e[o]; ++j) {
-            if ((uint32_t)j == i) continue;
-            const float3 d = sub3(pi, xyz(__ldg(P + j)));
-            const float r2 = dot3(d, d);
-            if (r2 > c.r2cut) continue;  // len > h: Wpoly6 = gradWspiky = 0
-            const float len = fsqrt(r2);
-            rho = fadd(rho, w_poly6(c, len));  // :80-82
-            if (len == 0.0f) continue;         // gradWspiky(0) = 0 (:60)
-            const float3 g = scale3(d, grad_scale(c.kg_lambda, c.h, len));  // :86-87
-            sumk = fadd(sumk, dot3(g, g));     // :89
-            gi = add3(gi, g);                  // :93
-        }
-    }
-    sumk = fadd(sumk, dot3(gi, gi));               // :97
-    const float Ci = ffma(rho, c.oorho, -1.0f);    // :100
-    const float lam = fdiv(-Ci, fadd(sumk, c.eps));  // :101
-    L[i] = make_float4(pi.x, pi.y, pi.z, lam);
+    runs_of(key, c, cstart, cend, r);
+#pragma unroll 1
+    for (int o = 0; o < 9; ++o)
+        for (int32_t j = r.b[o]; j < r.e[o]; ++j)
+            if ((uint32_t)j != i) f((uint32_t)j);
 }
 
-// updatepos.glsl:42-104.  Reads L = (p, lambda), writes clamped positions Pn.
-__global__ void __launch_bounds__(kBlock)
-k_delta_p(const float4* __restrict__ L, const uint32_t* __restrict__ skeys,
-          const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
-          float4* __restrict__ Pn, uint32_t n, DevConsts c, uint32_t* status) {
+template <class F>
+__device__ __forceinline__ void visit_list(uint32_t i, int32_t cnt, const NbrLists& nl, F&& f) {
+    const uint32_t* __restrict__ p = nl.idx + i;
+    for (int32_t k = 0; k < cnt; ++k) f(__ldg(p + (size_t)k * nl.n));
+}
+
+// Guard: may particle i (current position pi, predicted position xi) use
+// its list in a sweep whose positions have moved at most dmax from the
+// predicted ones?  NaN anywhere makes the answer false.
+__device__ __forceinline__ bool list_usable(const DevConsts& c, const NbrLists& nl, int32_t cnt,
+                                            float3 pi, float3 xi, int dmax_slot) {
+    if (!c.use_lists || cnt < 0) return false;
+    const float3 dd = make_float3(pi.x - xi.x, pi.y - xi.y, pi.z - xi.z);
+    const float di = sqrtf(dd.x * dd.x + dd.y * dd.y + dd.z * dd.z) * 1.0001f;
+    const float dmax = dmax_slot < 0 ? 0.0f : __uint_as_float(nl.guard[dmax_slot]) * 1.0001f;
+    const float coord = fmaxf(__uint_as_float(nl.guard[0]), c.wall_abs_max);
+    const float margin = c.margin_h + 16.0f * 5.9604645e-8f * coord;  // 16 ulp(coord)
+    return di + dmax + margin < c.skin;
+}
+
+__device__ __forceinline__ void warp_max_to(uint32_t* slot, float v) {
+    // v >= 0 or NaN; non-negative floats order like their bit patterns
+    uint32_t b = __float_as_uint(v);
+    for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(slot, b);
+}
+
+// ---- pair bodies (shared by both visitors) ---------------------------------------
+
+struct LambdaAcc {
+    float rho, sumk;
+    float3 gi;
+};
+
+// calclambda.glsl:75-95 for one neighbour at offset d = p_i - p_j, r2 = |d|^2.
+__device__ __forceinline__ void lambda_pair(const DevConsts& c, float3 d, float r2, LambdaAcc& a) {
+    if (r2 > c.r2cut) return;  // len > h: Wpoly6 = gradWspiky = 0
+    const float len = fsqrt(r2);
+    a.rho = fadd(a.rho, w_poly6(c, len));  // :80-82
+    if (len == 0.0f) return;               // gradWspiky(0) = 0 (:60)
+    const float3 g = scale3(d, grad_scale(c.kg_lambda, c.h, len));  // :86-87
+    a.sumk = fadd(a.sumk, dot3(g, g));     // :89
+    a.gi = add3(a.gi, g);                  // :93
+}
+
+// calclambda.glsl:97-101
+__device__ __forceinline__ float lambda_finish(const DevConsts& c, const LambdaAcc& a) {
+    const float sumk = fadd(a.sumk, dot3(a.gi, a.gi));  // :97
+    const float Ci = ffma(a.rho, c.oorho, -1.0f);        // :100
+    return fdiv(-Ci, fadd(sumk, c.eps));                 // :101
+}
+
+// ---- solver kernels --------------------------------------------------------------
+
+// Resident 256-thread blocks per SM the sweep kernels are compiled for (caps
+// them at 32 registers: full occupancy hides the gather and sqrt/div latency).
+constexpr int kSweepBlocksPerSM = 8;
+//
+// One thread per sorted particle; each walks its own candidates directly.
+// (A warp-lockstep scan with a shared-memory queue of in-range candidates was
+// measured ~10% slower on the 2M dam break and costs occupancy on the list
+// path, so the direct loop stays.)
+
+// First lambda sweep of a substep (calclambda.glsl:66-102) at the predicted
+// positions XP: a full stencil scan that also records, in visit order, every
+// candidate within h + skin (the neighbour list of the later sweeps) and the
+// largest coordinate magnitude (for the guard's rounding margin).
+__global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
+k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys,
+               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
+               float4* __restrict__ L, NbrLists nl, uint32_t n, DevConsts c) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < n;
+    float3 pi = make_float3(0.0f, 0.0f, 0.0f);
+    if (live) {
+        pi = xyz(XP[i]);
+        LambdaAcc a{0.0f, 0.0f, make_float3(0.0f, 0.0f, 0.0f)};
+        int32_t cnt = 0;
+        const uint32_t cap = c.use_lists ? nl.cap : 0u;
+        visit_full(i, skeys[i], c, cstart, cend, [&](uint32_t j) {
+            const float3 d = sub3(pi, xyz(__ldg(XP + j)));
+            const float r2 = dot3(d, d);
+            if (r2 <= c.r2list) {
+                if ((uint32_t)cnt < cap) nl.idx[(size_t)cnt * n + i] = j;
+                ++cnt;
+            }
+            lambda_pair(c, d, r2, a);
+        });
+        nl.cnt[i] = (uint32_t)cnt <= cap ? cnt : -1;
+        L[i] = make_float4(pi.x, pi.y, pi.z, lambda_finish(c, a));
+    }
+    const float m = fmaxf(fmaxf(fabsf(pi.x), fabsf(pi.y)), fabsf(pi.z));
+    warp_max_to(nl.guard, m);
+}
+
+// calclambda.glsl:66-102 at positions P (iterations after the first).
+// dmax_slot: guard slot holding the largest displacement of P from XP.
+__global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
+k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
+         const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cstart,
+         const int32_t* __restrict__ cend, float4* __restrict__ L, NbrLists nl, int dmax_slot,
+         uint32_t n, DevConsts c) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    Runs r;
-    runs_of(skeys[i], c, cstart, cend, r);
-    const float4 Li = L[i];
-    const float3 pi = xyz(Li);
-    const float li = Li.w;
-    float3 dp = make_float3(0.0f, 0.0f, 0.0f);
-    for (int o = 0; o < 9; ++o) {
-        for (int32_t j = r.b[o]; j < r.e[o]; ++j) {
-            if ((uint32_t)j == i) continue;
+    const float3 pi = xyz(P[i]);
+    LambdaAcc a{0.0f, 0.0f, make_float3(0.0f, 0.0f, 0.0f)};
+    auto body = [&](uint32_t j) {
+        const float3 d = sub3(pi, xyz(__ldg(P + j)));
+        lambda_pair(c, d, dot3(d, d), a);
+    };
+    const int32_t cnt = nl.cnt[i];
+    if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot))
+        visit_list(i, cnt, nl, body);
+    else
+        visit_full(i, skeys[i], c, cstart, cend, body);
+    L[i] = make_float4(pi.x, pi.y, pi.z, lambda_finish(c, a));
+}
+
+// updatepos.glsl:42-104.  Reads L = (p, lambda), writes clamped positions Pn
+// and the largest displacement of Pn from XP into guard slot `out_slot`.
+__global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
+k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
+          const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cstart,
+          const int32_t* __restrict__ cend, float4* __restrict__ Pn, NbrLists nl, int dmax_slot,
+          int out_slot, uint32_t n, DevConsts c, uint32_t* status) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < n;
+    float disp = 0.0f;
+    if (live) {
+        const float4 Li = L[i];
+        const float3 pi = xyz(Li);
+        const float li = Li.w;
+        float3 dp = make_float3(0.0f, 0.0f, 0.0f);
+        auto body = [&](uint32_t j) {
             const float4 Lj = __ldg(L + j);
             const float3 d = sub3(pi, xyz(Lj));
             const float r2 = dot3(d, d);
-            if (r2 > c.r2cut) continue;
+            if (r2 > c.r2cut) return;
             const float len = fsqrt(r2);
-            if (len == 0.0f) continue;
+            if (len == 0.0f) return;
             float sc = fmul(c.scale, w_poly6(c, len));  // :57
             sc = fmul(sc, sc);                           // :58
             sc = fmul(sc, sc);                           // :59
@@ -178,19 +291,28 @@ k_delta_p(const float4* __restrict__ L, const uint32_t* __restrict__ skeys,
             const float coef = fadd(fadd(li, Lj.w), sc); // :65
             const float3 g = scale3(d, grad_scale(c.kg, c.h, len));
             dp = fma3(coef, g, dp);                      // :65
-        }
+        };
+        const float3 xi = xyz(XP[i]);
+        const int32_t cnt = nl.cnt[i];
+        if (list_usable(c, nl, cnt, pi, xi, dmax_slot))
+            visit_list(i, cnt, nl, body);
+        else
+            visit_full(i, skeys[i], c, cstart, cend, body);
+        float3 q = fma3(c.oorho, dp, pi);  // :85
+        // clamp (:100) as min(max(q, lo), hi) with explicit selects, so signed
+        // zeros and NaN behave like the oracle's std::min/std::max
+        q.x = (q.x < c.lo[0]) ? c.lo[0] : q.x;
+        q.x = (c.hi[0] < q.x) ? c.hi[0] : q.x;
+        q.y = (q.y < c.lo[1]) ? c.lo[1] : q.y;
+        q.y = (c.hi[1] < q.y) ? c.hi[1] : q.y;
+        q.z = (q.z < c.lo[2]) ? c.lo[2] : q.z;
+        q.z = (c.hi[2] < q.z) ? c.hi[2] : q.z;
+        if (!finite3(q)) atomicOr(status, kDevNonFinite);
+        Pn[i] = make_float4(q.x, q.y, q.z, 0.0f);
+        const float3 dd = make_float3(q.x - xi.x, q.y - xi.y, q.z - xi.z);
+        disp = sqrtf(dd.x * dd.x + dd.y * dd.y + dd.z * dd.z);
     }
-    float3 q = fma3(c.oorho, dp, pi);  // :85
-    // clamp (:100) as min(max(q, lo), hi) with explicit selects, so signed
-    // zeros and NaN behave like the oracle's std::min/std::max
-    q.x = (q.x < c.lo[0]) ? c.lo[0] : q.x;
-    q.x = (c.hi[0] < q.x) ? c.hi[0] : q.x;
-    q.y = (q.y < c.lo[1]) ? c.lo[1] : q.y;
-    q.y = (c.hi[1] < q.y) ? c.hi[1] : q.y;
-    q.z = (q.z < c.lo[2]) ? c.lo[2] : q.z;
-    q.z = (c.hi[2] < q.z) ? c.hi[2] : q.z;
-    if (!finite3(q)) atomicOr(status, kDevNonFinite);
-    Pn[i] = make_float4(q.x, q.y, q.z, 0.0f);
+    warp_max_to(nl.guard + out_slot, disp);
 }
 
 // update.glsl:16-28: v = (x* - x_old) / dt, x = x*, scattered back to id order.
@@ -213,32 +335,34 @@ k_commit(const float4* __restrict__ P, const uint32_t* __restrict__ perm, float4
 
 // vorticity.glsl:34-60: XSPH velocity and the vorticity vector, Jacobi
 // (every read sees the committed velocities).
-__global__ void __launch_bounds__(kBlock)
-k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ VS,
-              const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cstart,
-              const int32_t* __restrict__ cend, float4* __restrict__ VX, float4* __restrict__ OM,
-              float4* __restrict__ Q, uint32_t n, DevConsts c) {
+__global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
+k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
+              const float4* __restrict__ VS, const uint32_t* __restrict__ skeys,
+              const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
+              float4* __restrict__ VX, float4* __restrict__ OM, float4* __restrict__ Q,
+              NbrLists nl, int dmax_slot, uint32_t n, DevConsts c) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    Runs r;
-    runs_of(skeys[i], c, cstart, cend, r);
     const float3 pi = xyz(P[i]);
     const float3 vi = xyz(VS[i]);
     float3 acc = make_float3(0.0f, 0.0f, 0.0f), w = make_float3(0.0f, 0.0f, 0.0f);
-    for (int o = 0; o < 9; ++o) {
-        for (int32_t j = r.b[o]; j < r.e[o]; ++j) {
-            if ((uint32_t)j == i) continue;
-            const float3 d = sub3(pi, xyz(__ldg(P + j)));  // :51
-            const float r2 = dot3(d, d);
-            if (r2 > c.r2cut) continue;
-            const float len = fsqrt(r2);
-            const float3 vij = sub3(xyz(__ldg(VS + j)), vi);  // :50
-            acc = fma3(w_poly6(c, len), vij, acc);            // :52-54
-            if (len == 0.0f) continue;
-            const float3 g = scale3(d, grad_scale(c.kg, c.h, len));
-            w = add3(w, cross3(vij, g));  // :55
-        }
-    }
+    auto pos = [&](uint32_t j) { return xyz(__ldg(P + j)); };
+    auto body = [&](uint32_t j) {
+        const float3 d = sub3(pi, pos(j));  // :51
+        const float r2 = dot3(d, d);
+        if (r2 > c.r2cut) return;
+        const float len = fsqrt(r2);
+        const float3 vij = sub3(xyz(__ldg(VS + j)), vi);  // :50
+        acc = fma3(w_poly6(c, len), vij, acc);            // :52-54
+        if (len == 0.0f) return;
+        const float3 g = scale3(d, grad_scale(c.kg, c.h, len));
+        w = add3(w, cross3(vij, g));  // :55
+    };
+    const int32_t cnt = nl.cnt[i];
+    if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot))
+        visit_list(i, cnt, nl, body);
+    else
+        visit_full(i, skeys[i], c, cstart, cend, body);
     const float3 vx = fma3(c.cx, acc, vi);  // :58
     VX[i] = make_float4(vx.x, vx.y, vx.z, 0.0f);
     OM[i] = make_float4(w.x, w.y, w.z, 0.0f);
@@ -247,29 +371,31 @@ k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ VS,
 
 // vorticity.glsl:65-85: confinement from the gradient of |vorticity|; writes
 // the final velocity in id order.
-__global__ void __launch_bounds__(kBlock)
-k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ VX,
-              const float4* __restrict__ OM, const uint32_t* __restrict__ skeys,
-              const uint32_t* __restrict__ perm, const int32_t* __restrict__ cstart,
-              const int32_t* __restrict__ cend, float4* __restrict__ v, uint32_t n, DevConsts c) {
+__global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
+k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ XP,
+              const float4* __restrict__ VX, const float4* __restrict__ OM,
+              const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
+              const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
+              float4* __restrict__ v, NbrLists nl, int dmax_slot, uint32_t n, DevConsts c) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    Runs r;
-    runs_of(skeys[i], c, cstart, cend, r);
     const float3 pi = xyz(Q[i]);
     float3 eta = make_float3(0.0f, 0.0f, 0.0f);
-    for (int o = 0; o < 9; ++o) {
-        for (int32_t j = r.b[o]; j < r.e[o]; ++j) {
-            if ((uint32_t)j == i) continue;
-            const float4 Qj = __ldg(Q + j);
-            const float3 d = sub3(pi, xyz(Qj));  // :69
-            const float r2 = dot3(d, d);
-            if (r2 > c.r2cut) continue;
-            const float len = fsqrt(r2);
-            if (len == 0.0f) continue;
-            eta = fma3(Qj.w, scale3(d, grad_scale(c.kg, c.h, len)), eta);  // :72
-        }
-    }
+    auto pos = [&](uint32_t j) { return xyz(__ldg(Q + j)); };
+    auto body = [&](uint32_t j) {
+        const float4 Qj = __ldg(Q + j);
+        const float3 d = sub3(pi, xyz(Qj));  // :69
+        const float r2 = dot3(d, d);
+        if (r2 > c.r2cut) return;
+        const float len = fsqrt(r2);
+        if (len == 0.0f) return;
+        eta = fma3(Qj.w, scale3(d, grad_scale(c.kg, c.h, len)), eta);  // :72
+    };
+    const int32_t cnt = nl.cnt[i];
+    if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot))
+        visit_list(i, cnt, nl, body);
+    else
+        visit_full(i, skeys[i], c, cstart, cend, body);
     const float l = fsqrt(dot3(eta, eta));  // :76
     if (l > 0.0f) eta = make_float3(fdiv(eta.x, l), fdiv(eta.y, l), fdiv(eta.z, l));  // :77-78
     const float3 vf = fma3(c.dteps, cross3(eta, xyz(OM[i])), xyz(VX[i]));  // :82

@@ -18,7 +18,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._capi import (PBF_DEVICE, PBF_HOST, Diagnostics, Params, PbfError, check, load)
+from ._capi import (PBF_DEVICE, PBF_HOST, Diagnostics, Params, PbfError, Tuning, check, load)
 
 
 def default_params(gridsize=(128, 64, 128)) -> Params:
@@ -161,6 +161,22 @@ class SPH:
     def SetExternalForce(self, state: bool) -> None:
         self._update(external_force=1 if state else 0)
 
+    # ---- tuning (no result depends on it) ---------------------------------
+    def get_tuning(self) -> Tuning:
+        t = Tuning()
+        check(self._lib.pbf_get_tuning(self._h, C.byref(t)), self._h)
+        return t
+
+    def set_tuning(self, use_neighbour_lists=None, list_capacity=None, skin_h=None) -> None:
+        t = self.get_tuning()
+        if use_neighbour_lists is not None:
+            t.use_neighbour_lists = 1 if use_neighbour_lists else 0
+        if list_capacity is not None:
+            t.list_capacity = int(list_capacity)
+        if skin_h is not None:
+            t.skin_h = float(skin_h)
+        check(self._lib.pbf_set_tuning(self._h, C.byref(t)), self._h)
+
     # ---- state ------------------------------------------------------------
     def set_state(self, x4, v4) -> None:
         """Uploads positions and velocities (id order, (n,4) or (n,3) float32)."""
@@ -226,6 +242,19 @@ class SPH:
         check(self._lib.pbf_get_timing(self._h, ms), self._h)
         names = ("predict", "sort", "neighbour_cells", "solver", "vorticity")
         return {k: float(v) for k, v in zip(names, ms)}
+
+    STAGES = ("predict", "sort", "cells", "lambda", "delta_p", "commit", "vorticity_a",
+              "vorticity_b")
+
+    def stage_times(self) -> tuple[dict, int]:
+        """Per-stage millisecond sums since EnableTiming, and the substep count."""
+        ms = (C.c_double * 8)()
+        cnt = C.c_uint32()
+        check(self._lib.pbf_get_stage_times(self._h, ms, C.byref(cnt)), self._h)
+        return {k: float(v) for k, v in zip(self.STAGES, ms)}, int(cnt.value)
+
+    def kernels_per_substep(self) -> int:
+        return int(self._lib.pbf_kernels_per_substep(self._h))
 
     # ---- debug reads of the last substep ---------------------------------------
     def get_sort(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:

@@ -220,3 +220,36 @@ def test_set_params_rejects_grid_change(gpu):
     p.grid[0] = 10
     with pytest.raises(pg.PbfError):
         g.set_params(p)
+
+
+@pytest.mark.parametrize("tuning", [dict(use_neighbour_lists=False),
+                                    dict(use_neighbour_lists=True, list_capacity=8),
+                                    dict(use_neighbour_lists=True, skin_h=0.0),
+                                    dict(use_neighbour_lists=True, skin_h=0.5, list_capacity=400),
+                                    dict(use_neighbour_lists=True, skin_h=0.02)])
+def test_tuning_never_changes_results(gpu, oracle_mod, tuning):
+    """Neighbour lists, their capacity and skin are performance knobs only."""
+    sc = scenes.plain_16k()
+    g = pg.SPH(sc.n, tuple(sc.params.grid), sc.params)
+    g.set_tuning(**tuning)
+    g.set_state(sc.x4, sc.v4)
+    g.step(30)
+    o = run_oracle(oracle_mod, sc.params, sc.x4, sc.v4, 30)
+    x, v = g.get_state()
+    ox, ov = o.get_state()
+    assert_bits(x, ox, f"positions with {tuning}")
+    assert_bits(v, ov, f"velocities with {tuning}")
+
+
+def test_lists_exact_in_a_calm_scene(gpu, oracle_mod):
+    """A stable scene (reference default epsilon = 5) where the lists are in use on
+    most sweeps, over many substeps."""
+    sc = scenes.plain_16k()
+    p = sc.params.copy()
+    p.epsilon = 5.0
+    g = run_gpu(p, sc.x4, sc.v4, 60)
+    o = run_oracle(oracle_mod, p, sc.x4, sc.v4, 60)
+    x, v = g.get_state()
+    ox, ov = o.get_state()
+    assert_bits(x, ox, "positions after 60 calm substeps")
+    assert_bits(v, ov, "velocities after 60 calm substeps")
