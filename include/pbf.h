@@ -224,6 +224,23 @@ pbf_status pbf_get_solver(pbf_sim* sim, float* lambda_sorted, float* xpred4_sort
 pbf_status pbf_radix_sort(const uint32_t* keys_in, uint32_t* keys_out, uint32_t* perm_out,
                           uint32_t n, uint32_t numbits, void* stream);
 
+/* Allocation-free variant of pbf_radix_sort, with the same arguments and
+ * results.  No counterpart in the reference (its RadixSort allocates its GL
+ * buffers in the constructor, where allocation is always allowed).  For
+ * callers that cannot call cudaMalloc: code running inside CUDA graph
+ * capture, a host application whose allocator owns all device memory, or a
+ * real-time loop that must not block on the allocator.  It allocates
+ * nothing: its scratch is one device array inside the library, sized for at
+ * most 1,048,576 keys (larger n returns PBF_ERR_INVALID_ARGUMENT), which every
+ * GPU that loads the library holds (about 13.6 MB) until the process exits.
+ * The first call on a device looks up that array's device address; make the
+ * first call on each device before any stream capture.  All calls share the
+ * array, so calls whose work overlaps on the GPU (other streams, other host
+ * threads) race and corrupt each other: serialise them.  Device pointers;
+ * runs on `stream` and synchronises before returning. */
+pbf_status pbf_radix_sort_noalloc(const uint32_t* keys_in, uint32_t* keys_out, uint32_t* perm_out,
+                                  uint32_t n, uint32_t numbits, void* stream);
+
 /* NeighbourCellFinder's findcells pass (shaders/neighbourcellfinder/findcells.glsl:34-53)
  * on n sorted keys below num_cells: fills start/end (num_cells entries each,
  * -1 for empty cells).  Device pointers; synchronises before returning. */

@@ -113,6 +113,7 @@ SIGNATURES = {
     "pbf_get_cells": (C.c_int, [_P, _P, _P]),
     "pbf_get_solver": (C.c_int, [_P, _P, _P]),
     "pbf_radix_sort": (C.c_int, [_P, _P, _P, C.c_uint32, C.c_uint32, _P]),
+    "pbf_radix_sort_noalloc": (C.c_int, [_P, _P, _P, C.c_uint32, C.c_uint32, _P]),
     "pbf_find_cells": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, _P]),
     "pbf_compute_diagnostics": (C.c_int, [_P, C.POINTER(Diagnostics)]),
     "pbf_status_string": (C.c_char_p, [C.c_int]),

@@ -13,6 +13,7 @@
 
 #include "../../include/pbf.h"
 #include "common.cuh"
+#include "internal.h"
 #include "sort.cuh"
 #include "substep.cuh"
 
@@ -23,6 +24,8 @@ namespace {
 thread_local std::string g_error;  // last error of calls without a handle
 
 }  // namespace
+
+void pbf::set_last_error(const char* msg) { g_error = msg ? msg : ""; }
 
 struct pbf_sim {
     int device = 0;

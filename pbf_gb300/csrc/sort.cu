@@ -18,6 +18,12 @@
 // order the reference's stable passes give on its id-ordered input.
 #include "sort.cuh"
 #include "common.cuh"
+#include "internal.h"
+
+#include <mutex>
+#include <string>
+
+#include "../../include/pbf.h"
 
 #include <algorithm>
 
@@ -29,6 +35,7 @@ constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kItems = 16;
 constexpr uint32_t kTile = kSortThreads * kItems;  // 4096 keys
+static_assert(kTile == kSortTile, "tile size");
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kValueMask = (1u << 30) - 1u;
@@ -226,16 +233,7 @@ uint32_t sort_numbits_for_cells(uint64_t ncells) {
     return r;
 }
 
-size_t SortWorkspace::bytes_for(uint32_t n) {
-    const uint64_t tiles = (n + kTile - 1) / kTile;
-    size_t b = 0;
-    b += sizeof(uint32_t) * kMaxPasses * 256;             // hist / digit base
-    b += sizeof(uint32_t) * kMaxPasses * 32;              // tile counters (padded)
-    b += sizeof(uint32_t) * kMaxPasses * 256 * tiles;     // lookback status
-    b = (b + 255) & ~size_t(255);
-    b += 2 * sizeof(uint32_t) * (size_t)n;                // ping-pong keys + values
-    return b;
-}
+size_t SortWorkspace::bytes_for(uint32_t n) { return sort_ws_bytes(n); }
 
 void SortWorkspace::carve(void* base, uint32_t n) {
     capacity = n;
@@ -284,3 +282,93 @@ cudaError_t sort_pairs(const SortWorkspace& ws, const uint32_t* keys_in, uint32_
 }
 
 }  // namespace pbf
+
+// ---- allocation-free variant -------------------------------------------------
+//
+// For callers that must not allocate device memory: a library embedded in a
+// host application whose allocator owns all of the GPU's memory, code that
+// runs while a CUDA graph is being captured (where cudaMalloc is not
+// allowed), or a real-time loop that may not block on the allocator.  The
+// sort's scratch (digit histograms, lookback status, ping-pong buffers, a key
+// buffer for callers that want no sorted keys, the status word) lives in one
+// file-scope device array sized for at most kNoAllocMaxKeys keys.  Every GPU
+// that loads the library holds this array (about 13.6 MB) until the process
+// exits.
+
+static constexpr uint32_t kNoAllocMaxKeys = 1u << 20;
+static constexpr size_t kNoAllocWsBytes = pbf::sort_ws_bytes(kNoAllocMaxKeys);
+static constexpr size_t kNoAllocBytes =
+    kNoAllocWsBytes + sizeof(uint32_t) * kNoAllocMaxKeys + 256;  // + key buffer + status
+static constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) uint8_t g_sort_scratch[kNoAllocBytes];
+
+// Host code cannot use g_sort_scratch's name as a device address; the address
+// is looked up once per device (with that device current) and cached.
+static std::mutex g_sort_scratch_mu;
+static void* g_sort_scratch_addr[kNoAllocMaxDevices] = {};
+
+static cudaError_t sort_scratch_address(int dev, void** out) {
+    std::lock_guard<std::mutex> lock(g_sort_scratch_mu);
+    if (!g_sort_scratch_addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_sort_scratch);
+        if (e != cudaSuccess) return e;
+        g_sort_scratch_addr[dev] = p;
+    }
+    *out = g_sort_scratch_addr[dev];
+    return cudaSuccess;
+}
+
+static pbf_status noalloc_fail(pbf_status st, const std::string& msg) {
+    pbf::set_last_error(msg.c_str());
+    return st;
+}
+
+extern "C" pbf_status pbf_radix_sort_noalloc(const uint32_t* keys_in, uint32_t* keys_out,
+                                             uint32_t* perm_out, uint32_t n, uint32_t numbits,
+                                             void* stream) {
+    if (n == 0) return PBF_OK;
+    if (!keys_in || !perm_out)
+        return noalloc_fail(PBF_ERR_INVALID_ARGUMENT, "keys_in and perm_out are required");
+    if (numbits < 1 || numbits > 32)
+        return noalloc_fail(PBF_ERR_INVALID_ARGUMENT, "numbits must be in [1, 32]");
+    if (n > kNoAllocMaxKeys)
+        return noalloc_fail(PBF_ERR_INVALID_ARGUMENT,
+                            "n = " + std::to_string(n) +
+                                " exceeds the allocation-free sort's limit of " +
+                                std::to_string(kNoAllocMaxKeys) + " keys");
+    if ((const void*)perm_out == (const void*)keys_in ||
+        (keys_out && (const void*)keys_out == (const void*)keys_in))
+        return noalloc_fail(PBF_ERR_INVALID_ARGUMENT, "outputs must not alias keys_in");
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return noalloc_fail(PBF_ERR_NO_DEVICE, "no CUDA device");
+    }
+    if (dev < 0 || dev >= kNoAllocMaxDevices)
+        return noalloc_fail(PBF_ERR_UNSUPPORTED, "device ordinal above 63");
+    void* base = nullptr;
+    cudaError_t e = sort_scratch_address(dev, &base);
+    if (e != cudaSuccess)
+        return noalloc_fail(PBF_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    pbf::SortWorkspace ws;
+    ws.carve(base, kNoAllocMaxKeys);
+    uint32_t* key_buf = (uint32_t*)((uint8_t*)base + kNoAllocWsBytes);
+    uint32_t* status = key_buf + kNoAllocMaxKeys;
+    uint32_t* kout = keys_out ? keys_out : key_buf;
+    cudaStream_t st = (cudaStream_t)stream;
+    // The array keeps the previous call's contents: the status word is
+    // cleared here and sort_pairs clears its histograms, tile counters and
+    // lookback words before use.
+    uint32_t bits = 0;
+    e = cudaMemsetAsync(status, 0, sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = pbf::sort_pairs(ws, keys_in, kout, perm_out, n, numbits, status, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bits, status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess)
+        return noalloc_fail(PBF_ERR_CUDA, std::string("pbf_radix_sort_noalloc: ") + cudaGetErrorString(e));
+    if (bits & pbf::kDevSortTimeout)
+        return noalloc_fail(PBF_ERR_DEVICE_FAULT, "radix-sort lookback timed out");
+    return PBF_OK;
+}

@@ -7,7 +7,18 @@
 
 namespace pbf {
 
-constexpr uint32_t kMaxPasses = 4;  // 8-bit digits, 32-bit keys
+constexpr uint32_t kMaxPasses = 4;     // 8-bit digits, 32-bit keys
+constexpr uint32_t kSortTile = 4096;   // keys per onesweep tile
+
+// Bytes of the workspace SortWorkspace::carve lays out for up to n keys.
+constexpr size_t sort_ws_bytes(uint32_t n) {
+    const size_t tiles = ((size_t)n + kSortTile - 1) / kSortTile;
+    size_t b = sizeof(uint32_t) * kMaxPasses * 256        // hist / digit base
+               + sizeof(uint32_t) * kMaxPasses * 32       // tile counters (padded)
+               + sizeof(uint32_t) * kMaxPasses * 256 * tiles;  // lookback status
+    b = (b + 255) & ~size_t(255);
+    return b + 2 * sizeof(uint32_t) * (size_t)n;          // ping-pong keys + values
+}
 
 // Device scratch of one sort: digit histograms, per-pass tile counters and
 // lookback status words (reset before every sort), and ping-pong buffers.
