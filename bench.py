@@ -61,6 +61,7 @@ def parse():
                     help="full substeps of the CPU baseline sample")
     ap.add_argument("--e2e-steps", type=int, default=0, help="0: min(steps, 50)")
     ap.add_argument("--no-stable", action="store_true", help="skip the epsilon = 5 full run")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 256-scene comparison")
     return ap.parse_args()
 
 
@@ -142,6 +143,64 @@ def profiled_traffic():
             return json.load(f)
     except Exception:
         return None
+
+
+def batched_vs_plain(stream, num_scenes: int = 256, substeps: int = 100):
+    """256 dam breaks (4,096-65,536 particles, boxes 32-96 cells, 4 iterations,
+    100 substeps): one batched handle (every stage one launch over all scenes,
+    the substep replayed as one CUDA graph) against the same scenes stepped
+    one at a time, each in its own handle with its own graph, on the same
+    stream.  Both start from the initial scenes after 3 warm-up substeps."""
+    import torch
+    import numpy as np
+    import pbf_gb300 as pg
+    from pbf_gb300 import scenes
+    scs = scenes.batch_scenes(num_scenes, substeps=substeps)
+    x4, v4 = scenes.concat_state(scs)
+    batch = pg.SPHBatch([s.params for s in scs], [s.n for s in scs])
+    batch.set_stream(stream.cuda_stream)
+    batch.set_state(x4, v4)
+    batch.step(3)
+    batch.set_state(x4, v4)
+    plain = []
+    for s in scs:
+        h = pg.SPH(s.n, tuple(s.params.grid), s.params)
+        h.set_stream(stream.cuda_stream)
+        h.set_state(s.x4, s.v4)
+        h.step(3)
+        h.set_state(s.x4, s.v4)
+        plain.append(h)
+    torch.cuda.synchronize()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    e[0].record(stream)
+    batch.step(substeps)
+    e[1].record(stream)
+    torch.cuda.synchronize()
+    e[2].record(stream)
+    for h in plain:
+        h.step(substeps)
+    e[3].record(stream)
+    torch.cuda.synchronize()
+    tb = e[0].elapsed_time(e[1])
+    tp = e[2].elapsed_time(e[3])
+    bx, bv = batch.get_state()
+    same = True
+    for k in range(0, num_scenes, max(1, num_scenes // 16)):
+        px, pv = plain[k].get_state()
+        sl = batch.scene_slice(k)
+        same = same and np.array_equal(bx[sl].view(np.uint32), px.view(np.uint32)) and \
+            np.array_equal(bv[sl].view(np.uint32), pv.view(np.uint32))
+    n = int(x4.shape[0])
+    it = scs[0].params.num_solver_iterations
+    for h in plain:
+        h.close()
+    batch.close()
+    return {"scenes": num_scenes, "particles": n, "substeps": substeps,
+            "batched_ms": tb, "plain_ms": tp,
+            "batched_scenes_per_s": num_scenes / (tb * 1e-3),
+            "plain_scenes_per_s": num_scenes / (tp * 1e-3), "speedup": tp / tb,
+            "batched_particle_iters_per_s": n * it * substeps / (tb * 1e-3),
+            "bit_identical_sampled_scenes": bool(same)}
 
 
 def cpu_baseline(scene, substeps: int):
@@ -326,6 +385,12 @@ def main():
                                           "(src/SPH.cpp:138), full run"}
         sim.set_params(scene.params)
 
+    batched = None
+    if not args.no_batched:
+        sim.close()
+        torch.cuda.empty_cache()
+        batched = batched_vs_plain(stream)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(scene, args.cpu_substeps)
@@ -353,6 +418,7 @@ def main():
             "kernel_share": {k: v / total_stage for k, v in stages.items()},
             "gpu_launches": launches,
             "stable_500": stable,
+            "batched_256": batched,
             "clocks": clk,
             "cpu_baseline": cpu,
         }

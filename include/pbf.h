@@ -119,11 +119,32 @@ pbf_status pbf_scene_block(const uint32_t lattice[3], float spacing, const float
  * needs a multiple of 512).  Uses the current CUDA device. */
 pbf_status pbf_create(const pbf_params* params, uint32_t n, pbf_sim** out);
 
+/* Several independent scenes in one handle (no reference counterpart: the
+ * reference steps one scene).  Scene k has scene_counts[k] particles and its
+ * own parameters (grid, walls, constants); all scenes share the iteration
+ * count and the vorticity flag.  Particle state is the scenes' float4 arrays
+ * concatenated in scene order; every other call (state, stepping, timing,
+ * tuning, debug reads) works on a batch as on a single scene, and each stage
+ * is one launch over all scenes.  A scene in a batch steps bit-identically to
+ * the same scene in its own handle. */
+pbf_status pbf_create_batch(const pbf_params* scene_params, const uint32_t* scene_counts,
+                            uint32_t num_scenes, pbf_sim** out);
+uint32_t pbf_num_scenes(const pbf_sim* sim);
+/* First particle and particle count of a scene in the concatenated arrays. */
+pbf_status pbf_scene_range(const pbf_sim* sim, uint32_t scene, uint32_t* first, uint32_t* count);
+/* Parameters of one scene (the grid must not change). */
+pbf_status pbf_set_scene_params(pbf_sim* sim, uint32_t scene, const pbf_params* params);
+pbf_status pbf_get_scene_params(const pbf_sim* sim, uint32_t scene, pbf_params* out);
+/* Cells of all scenes: the length of the pbf_get_cells tables. */
+uint32_t pbf_num_cells(const pbf_sim* sim);
+
 /* SPH::~SPH (src/SPH.h:43, src/SPH.cpp:153-157). */
 void pbf_destroy(pbf_sim* sim);
 
 /* All SPH::Set* parameter setters at once (src/SPH.cpp:166-204, uploaded by
- * SPH::UploadSPHParams :206-216).  The grid must not change. */
+ * SPH::UploadSPHParams :206-216).  The grid must not change.  Single-scene
+ * handles only (a batch takes pbf_set_scene_params); pbf_get_params returns
+ * scene 0's parameters. */
 pbf_status pbf_set_params(pbf_sim* sim, const pbf_params* params);
 pbf_status pbf_get_params(const pbf_sim* sim, pbf_params* out);
 uint32_t pbf_num_particles(const pbf_sim* sim);
@@ -206,7 +227,8 @@ pbf_status pbf_get_sort(pbf_sim* sim, uint32_t* keys_by_id, uint32_t* sorted_key
 
 /* Dense cell tables of NeighbourCellFinder (findcells.glsl:34-53):
  * start[c] = first sorted index in cell c, end[c] = one past its last, both
- * -1 for empty cells.  Each array has grid[0]*grid[1]*grid[2] entries. */
+ * -1 for empty cells.  Each array has pbf_num_cells() entries (the scenes'
+ * grids one after the other). */
 pbf_status pbf_get_cells(pbf_sim* sim, int32_t* start, int32_t* end);
 
 /* Lambda of the last solver iteration and the predicted positions (float4,

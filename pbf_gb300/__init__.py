@@ -7,8 +7,8 @@ Python host mirror of the reference's interface.
 """
 from ._capi import (PBF_DEV_NONFINITE, PBF_DEV_RUN_OVER_127, PBF_DEV_SORT_TIMEOUT, PBF_DEVICE,
                     PBF_HOST, Params, PbfError, load)
-from .sph import SPH, default_params
+from .sph import SPH, SPHBatch, default_params
 from . import scenes
 
-__all__ = ["SPH", "Params", "PbfError", "default_params", "load", "scenes", "PBF_HOST",
+__all__ = ["SPH", "SPHBatch", "Params", "PbfError", "default_params", "load", "scenes", "PBF_HOST",
            "PBF_DEVICE", "PBF_DEV_NONFINITE", "PBF_DEV_SORT_TIMEOUT", "PBF_DEV_RUN_OVER_127"]

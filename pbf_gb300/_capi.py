@@ -92,6 +92,12 @@ SIGNATURES = {
     "pbf_scene_block": (C.c_int, [_U32P, C.c_float, _F, C.c_float, C.c_float, C.c_float,
                                   C.c_uint64, _P, _P]),
     "pbf_create": (C.c_int, [C.POINTER(Params), C.c_uint32, C.POINTER(C.c_void_p)]),
+    "pbf_create_batch": (C.c_int, [C.POINTER(Params), _U32P, C.c_uint32, C.POINTER(C.c_void_p)]),
+    "pbf_num_scenes": (C.c_uint32, [_P]),
+    "pbf_scene_range": (C.c_int, [_P, C.c_uint32, _U32P, _U32P]),
+    "pbf_set_scene_params": (C.c_int, [_P, C.c_uint32, C.POINTER(Params)]),
+    "pbf_get_scene_params": (C.c_int, [_P, C.c_uint32, C.POINTER(Params)]),
+    "pbf_num_cells": (C.c_uint32, [_P]),
     "pbf_destroy": (None, [_P]),
     "pbf_set_params": (C.c_int, [_P, C.POINTER(Params)]),
     "pbf_get_params": (C.c_int, [_P, C.POINTER(Params)]),

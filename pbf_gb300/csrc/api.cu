@@ -31,11 +31,19 @@ struct pbf_sim {
     int device = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
-    pbf_params params{};
-    DevConsts dc{};
+    pbf_params params{};  // scene 0; its iteration count and vorticity flag hold for all scenes
+    DevConsts dc{};       // scene 0's constants (the kernel parameter of a single scene)
     uint32_t n = 0;
-    uint32_t ncells = 0;
+    uint32_t ncells = 0;  // all scenes
     uint32_t numbits = 0;
+    // several scenes in one handle (pbf_create_batch): concatenated scene-major
+    uint32_t nscenes = 1;
+    std::vector<pbf_params> sparams;
+    std::vector<DevConsts> sdc;
+    std::vector<uint32_t> counts, offsets;
+    DevConsts* d_consts = nullptr;  // [nscenes]
+    uint32_t* sid = nullptr;        // scene of each particle, id order
+    uint32_t* sid_sorted = nullptr; // scene of each particle, sorted order
 
     // id-order state and predicted positions
     float4 *x = nullptr, *v = nullptr, *xstar = nullptr;
@@ -234,7 +242,7 @@ void free_sim(pbf_sim* s) {
     void* bufs[] = {s->x,  s->v,  s->xstar, s->XP,   s->Pa,     s->Pb,   s->L,
                     s->VS, s->VX, s->OM,    s->Q,    s->keys,   s->skeys, s->perm,
                     s->cstart, s->cend, s->status, s->sort_mem, s->nbr_idx, s->nbr_cnt,
-                    s->guard};
+                    s->guard, s->d_consts, s->sid, s->sid_sorted};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (s->h_status) cudaFreeHost(s->h_status);
@@ -270,12 +278,12 @@ uint32_t kernels_per_substep(const pbf_sim* s) {
 // `ev` non-null, records an event at every stage boundary: before predict,
 // after predict, sort, cells, each lambda and delta-p launch, commit and the
 // two vorticity passes (7 + 2 * iterations events).
-cudaError_t enqueue_substep(pbf_sim* s, cudaEvent_t* ev) {
+template <class CPi, class CPs>
+cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const CPi& cpi, const CPs& cps) {
     const uint32_t n = s->n;
     if (!s->nbr_cnt || s->guard_slots < 2 + s->params.num_solver_iterations)
         return cudaErrorInvalidValue;  // ensure_lists() runs before any capture
     const unsigned g = grid_for(n);
-    const DevConsts& c = s->dc;
     const uint32_t iters = s->params.num_solver_iterations;
     cudaStream_t st = s->stream;
     auto mark = [&](uint32_t idx) {
@@ -283,7 +291,7 @@ cudaError_t enqueue_substep(pbf_sim* s, cudaEvent_t* ev) {
     };
     mark(0);
     // 1 predict (predictpos.glsl)
-    k_predict<<<g, kBlock, 0, st>>>(s->x, s->v, s->xstar, s->keys, n, c, s->status);
+    launch_predict(g, st, s->x, s->v, s->xstar, s->keys, n, cpi, s->status);
     mark(1);
     // 2 sort (RadixSort::Run); first clear the cell starts of the previous
     // substep while its sorted keys are still there
@@ -293,13 +301,11 @@ cudaError_t enqueue_substep(pbf_sim* s, cudaEvent_t* ev) {
     mark(2);
     // 3 cell ranges (NeighbourCellFinder::FindNeighbourCells)
     k_find_cells<<<g, kBlock, 0, st>>>(s->skeys, s->perm, s->xstar, s->XP, n, s->ncells, s->cstart,
-                                       s->cend, s->status + 1);
+                                       s->cend, s->status + 1, s->sid, s->sid_sorted);
     mark(3);
     // 4 solver iterations (calclambda / updatepos).  The first lambda sweep
     // also records the neighbour lists the later sweeps replay.
     const NbrLists nl{s->nbr_idx, s->nbr_cnt, s->guard, s->nbr_cap, n};
-    DevConsts cv = c;  // without iterations no list is built this substep
-    if (iters == 0) cv.use_lists = 0;
     cudaError_t ge = cudaMemsetAsync(s->guard, 0, sizeof(uint32_t) * (2 + iters), st);
     if (ge != cudaSuccess) return ge;
     const float4* cur = s->XP;
@@ -307,30 +313,36 @@ cudaError_t enqueue_substep(pbf_sim* s, cudaEvent_t* ev) {
         float4* nxt = (it % 2 == 0) ? s->Pa : s->Pb;
         const int in_slot = it == 0 ? -1 : (int)it;  // displacement of `cur` from XP
         if (it == 0)
-            k_lambda_build<<<g, kBlock, 0, st>>>(s->XP, s->skeys, s->cstart, s->cend, s->L, nl, n, c);
+            launch_lambda_build(g, st, s->XP, s->skeys, s->cstart, s->cend, s->L, nl, n, cps);
         else
-            k_lambda<<<g, kBlock, 0, st>>>(cur, s->XP, s->skeys, s->cstart, s->cend, s->L, nl,
-                                           in_slot, n, c);
+            launch_lambda(g, st, cur, s->XP, s->skeys, s->cstart, s->cend, s->L, nl,
+                                           in_slot, n, cps);
         mark(4 + 2 * it);
-        k_delta_p<<<g, kBlock, 0, st>>>(s->L, s->XP, s->skeys, s->cstart, s->cend, nxt, nl, in_slot,
-                                        (int)it + 1, n, c, s->status);
+        launch_delta_p(g, st, s->L, s->XP, s->skeys, s->cstart, s->cend, nxt, nl, in_slot,
+                                        (int)it + 1, n, cps, s->status);
         mark(5 + 2 * it);
         cur = nxt;
     }
     // 5 commit (update.glsl) and XSPH + vorticity (vorticity.glsl)
     const bool vort = s->params.vorticity_confinement != 0;
-    const int fin_slot = iters == 0 ? -1 : (int)iters;
-    k_commit<<<g, kBlock, 0, st>>>(cur, s->perm, s->x, s->VS, vort ? nullptr : s->v, n, c);
+    const int fin_slot = iters == 0 ? -2 : (int)iters;  // -2: no list was built this substep
+    launch_commit(g, st, cur, s->perm, s->x, s->VS, vort ? nullptr : s->v, n, cps);
     mark(4 + 2 * iters);
     if (vort)
-        k_vorticity_a<<<g, kBlock, 0, st>>>(cur, s->XP, s->VS, s->skeys, s->cstart, s->cend, s->VX,
-                                            s->OM, s->Q, nl, fin_slot, n, cv);
+        launch_vorticity_a(g, st, cur, s->XP, s->VS, s->skeys, s->cstart, s->cend, s->VX,
+                                            s->OM, s->Q, nl, fin_slot, n, cps);
     mark(5 + 2 * iters);
     if (vort)
-        k_vorticity_b<<<g, kBlock, 0, st>>>(s->Q, s->XP, s->VX, s->OM, s->skeys, s->perm, s->cstart,
-                                            s->cend, s->v, nl, fin_slot, n, cv);
+        launch_vorticity_b(g, st, s->Q, s->XP, s->VX, s->OM, s->skeys, s->perm, s->cstart,
+                                            s->cend, s->v, nl, fin_slot, n, cps);
     mark(6 + 2 * iters);
     return cudaGetLastError();
+}
+
+cudaError_t enqueue_substep(pbf_sim* s, cudaEvent_t* ev) {
+    if (s->nscenes == 1) return enqueue_impl(s, ev, OneScene{s->dc}, OneScene{s->dc});
+    return enqueue_impl(s, ev, ManyScenes{s->d_consts, s->sid},
+                        ManyScenes{s->d_consts, s->sid_sorted});
 }
 
 // One eager substep with stage events; accumulates the stage sums.
@@ -398,31 +410,69 @@ pbf_status timed_substep(pbf_sim* s) {
 extern "C" {
 
 pbf_status pbf_create(const pbf_params* params, uint32_t n, pbf_sim** out) {
+    return pbf_create_batch(params, &n, 1, out);
+}
+
+pbf_status pbf_create_batch(const pbf_params* scene_params, const uint32_t* scene_counts,
+                            uint32_t num_scenes, pbf_sim** out) {
     if (!out) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "out is NULL");
     *out = nullptr;
+    if (!scene_params || !scene_counts || num_scenes == 0)
+        return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "scene_params, scene_counts and num_scenes are required");
     std::string why;
-    if (validate_params(params, why) != PBF_OK) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, why);
-    if (n == 0 || n >= (1u << 30)) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "n must be in [1, 2^30)");
+    uint64_t total = 0, cells = 0;
+    for (uint32_t k = 0; k < num_scenes; ++k) {
+        if (validate_params(&scene_params[k], why) != PBF_OK)
+            return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "scene " + std::to_string(k) + ": " + why);
+        if (scene_counts[k] == 0)
+            return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "every scene needs at least one particle");
+        if (scene_params[k].num_solver_iterations != scene_params[0].num_solver_iterations ||
+            (scene_params[k].vorticity_confinement != 0) != (scene_params[0].vorticity_confinement != 0))
+            return fail(nullptr, PBF_ERR_INVALID_ARGUMENT,
+                        "all scenes share the iteration count and the vorticity flag");
+        total += scene_counts[k];
+        cells += (uint64_t)scene_params[k].grid[0] * scene_params[k].grid[1] * scene_params[k].grid[2];
+    }
+    if (total >= (1u << 30)) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "n must be in [1, 2^30)");
+    if (cells > 0x7FFFFFFFull) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "more than 2^31-1 cells in total");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();
         return fail(nullptr, PBF_ERR_NO_DEVICE, "no CUDA device");
     }
+    const uint32_t n = (uint32_t)total;
     pbf_sim* s = new pbf_sim();
     cudaGetDevice(&s->device);
-    s->params = *params;
+    s->nscenes = num_scenes;
+    s->sparams.assign(scene_params, scene_params + num_scenes);
+    s->counts.assign(scene_counts, scene_counts + num_scenes);
+    s->params = scene_params[0];
     s->tuning = default_tuning();
-    s->dc = make_consts(*params);
-    apply_tuning(s->dc, s->params, s->tuning);
     s->n = n;
-    s->ncells = params->grid[0] * params->grid[1] * params->grid[2];
+    s->ncells = (uint32_t)cells;
     s->numbits = sort_numbits_for_cells(s->ncells);
+    s->sdc.resize(num_scenes);
+    s->offsets.resize(num_scenes + 1);
+    uint32_t base = 0, off = 0;
+    for (uint32_t k = 0; k < num_scenes; ++k) {
+        s->sdc[k] = make_consts(scene_params[k]);
+        s->sdc[k].cell_base = base;
+        apply_tuning(s->sdc[k], scene_params[k], s->tuning);
+        base += s->sdc[k].ncells;
+        s->offsets[k] = off;
+        off += scene_counts[k];
+    }
+    s->offsets[num_scenes] = off;
+    s->dc = s->sdc[0];
     cudaError_t e = cudaSuccess;
 #define ALLOC(ptr, cnt)                                                  \
     if (e == cudaSuccess) e = dalloc(&s->ptr, (cnt));
     ALLOC(x, n) ALLOC(v, n) ALLOC(xstar, n) ALLOC(XP, n) ALLOC(Pa, n) ALLOC(Pb, n) ALLOC(L, n)
     ALLOC(VS, n) ALLOC(VX, n) ALLOC(OM, n) ALLOC(Q, n) ALLOC(keys, n) ALLOC(skeys, n)
     ALLOC(perm, n) ALLOC(cstart, s->ncells) ALLOC(cend, s->ncells) ALLOC(status, 2)
+    if (num_scenes > 1) {
+        ALLOC(d_consts, num_scenes) ALLOC(sid, n) ALLOC(sid_sorted, n)
+    }
 #undef ALLOC
     if (e == cudaSuccess) e = cudaMalloc(&s->sort_mem, SortWorkspace::bytes_for(n));
     if (e == cudaSuccess) e = ensure_lists(s);
@@ -443,6 +493,15 @@ pbf_status pbf_create(const pbf_params* params, uint32_t n, pbf_sim** out) {
     if (e == cudaSuccess) e = cudaMemsetAsync(s->x, 0, sizeof(float4) * n, s->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(s->v, 0, sizeof(float4) * n, s->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(s->status, 0, 2 * sizeof(uint32_t), s->stream);
+    if (e == cudaSuccess && num_scenes > 1) {
+        std::vector<uint32_t> sid(n);
+        for (uint32_t k = 0; k < num_scenes; ++k)
+            for (uint32_t i = s->offsets[k]; i < s->offsets[k + 1]; ++i) sid[i] = k;
+        e = cudaMemcpy(s->sid, sid.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(s->d_consts, s->sdc.data(), sizeof(DevConsts) * num_scenes,
+                           cudaMemcpyHostToDevice);
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     if (e != cudaSuccess) {
         pbf_status st = cuda_fail(nullptr, e, "pbf_create initialisation");
@@ -457,18 +516,57 @@ void pbf_destroy(pbf_sim* s) { free_sim(s); }
 
 pbf_status pbf_set_params(pbf_sim* s, const pbf_params* p) {
     if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
+    if (s->nscenes != 1)
+        return fail(s, PBF_ERR_INVALID_ARGUMENT, "a batch takes pbf_set_scene_params");
+    return pbf_set_scene_params(s, 0, p);
+}
+
+pbf_status pbf_set_scene_params(pbf_sim* s, uint32_t scene, const pbf_params* p) {
+    if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
+    if (scene >= s->nscenes) return fail(s, PBF_ERR_INVALID_ARGUMENT, "scene index out of range");
     std::string why;
     if (validate_params(p, why) != PBF_OK) return fail(s, PBF_ERR_INVALID_ARGUMENT, why);
     for (int a = 0; a < 3; ++a)
-        if (p->grid[a] != s->params.grid[a])
+        if (p->grid[a] != s->sparams[scene].grid[a])
             return fail(s, PBF_ERR_INVALID_ARGUMENT, "the grid is fixed at creation");
-    s->params = *p;
-    s->dc = make_consts(*p);
-    apply_tuning(s->dc, s->params, s->tuning);
-    invalidate_graph(s);
+    if (s->nscenes > 1 &&
+        (p->num_solver_iterations != s->params.num_solver_iterations ||
+         (p->vorticity_confinement != 0) != (s->params.vorticity_confinement != 0)))
+        return fail(s, PBF_ERR_INVALID_ARGUMENT,
+                    "all scenes share the iteration count and the vorticity flag");
     DeviceGuard dg(s->device);
     PBF_CUDA(s, cudaStreamSynchronize(s->stream));
+    const uint32_t base = s->sdc[scene].cell_base;
+    s->sparams[scene] = *p;
+    s->sdc[scene] = make_consts(*p);
+    s->sdc[scene].cell_base = base;
+    apply_tuning(s->sdc[scene], *p, s->tuning);
+    if (scene == 0) {
+        s->params = *p;
+        s->dc = s->sdc[0];
+    }
+    if (s->nscenes > 1)
+        PBF_CUDA(s, cudaMemcpy(s->d_consts + scene, &s->sdc[scene], sizeof(DevConsts),
+                               cudaMemcpyHostToDevice));
+    invalidate_graph(s);
     PBF_CUDA(s, ensure_lists(s));
+    return PBF_OK;
+}
+
+pbf_status pbf_get_scene_params(const pbf_sim* s, uint32_t scene, pbf_params* out) {
+    if (!s || !out) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (scene >= s->nscenes) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "scene index out of range");
+    *out = s->sparams[scene];
+    return PBF_OK;
+}
+
+uint32_t pbf_num_scenes(const pbf_sim* s) { return s ? s->nscenes : 0; }
+uint32_t pbf_num_cells(const pbf_sim* s) { return s ? s->ncells : 0; }
+
+pbf_status pbf_scene_range(const pbf_sim* s, uint32_t scene, uint32_t* first, uint32_t* count) {
+    if (!s || scene >= s->nscenes) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "bad scene");
+    if (first) *first = s->offsets[scene];
+    if (count) *count = s->counts[scene];
     return PBF_OK;
 }
 
@@ -481,7 +579,11 @@ pbf_status pbf_set_tuning(pbf_sim* s, const pbf_tuning* t) {
     DeviceGuard dg(s->device);
     PBF_CUDA(s, cudaStreamSynchronize(s->stream));
     s->tuning = *t;
-    apply_tuning(s->dc, s->params, s->tuning);
+    for (uint32_t k = 0; k < s->nscenes; ++k) apply_tuning(s->sdc[k], s->sparams[k], s->tuning);
+    s->dc = s->sdc[0];
+    if (s->nscenes > 1)
+        PBF_CUDA(s, cudaMemcpy(s->d_consts, s->sdc.data(), sizeof(DevConsts) * s->nscenes,
+                               cudaMemcpyHostToDevice));
     invalidate_graph(s);
     PBF_CUDA(s, ensure_lists(s));
     return PBF_OK;
@@ -661,13 +763,20 @@ pbf_status pbf_compute_diagnostics(pbf_sim* s, pbf_diagnostics* out) {
     const unsigned g = grid_for(n);
     cudaStream_t st = s->stream;
     k_unmark_cells<<<g, kBlock, 0, st>>>(s->skeys, n, s->ncells, s->cstart);
-    k_keys_of<<<g, kBlock, 0, st>>>(s->x, s->xstar, s->keys, n, s->dc);
+    if (s->nscenes == 1)
+        launch_keys_of(g, st, s->x, s->xstar, s->keys, n, OneScene{s->dc});
+    else
+        launch_keys_of(g, st, s->x, s->xstar, s->keys, n, ManyScenes{s->d_consts, s->sid});
     cudaError_t e = sort_pairs(s->sort, s->keys, s->skeys, s->perm, n, s->numbits, s->status, st);
     if (e != cudaSuccess) return cuda_fail(s, e, "diagnostics sort");
     k_find_cells<<<g, kBlock, 0, st>>>(s->skeys, s->perm, s->xstar, s->XP, n, s->ncells, s->cstart,
-                                       s->cend, s->status + 1);
-    k_diagnostics<<<g, kBlock, 0, st>>>(s->XP, s->v, s->skeys, s->perm, s->cstart, s->cend, s->VX,
-                                        n, s->dc);
+                                       s->cend, s->status + 1, s->sid, s->sid_sorted);
+    if (s->nscenes == 1)
+        launch_diagnostics(g, st, s->XP, s->v, s->skeys, s->perm, s->cstart, s->cend,
+                                            s->VX, n, OneScene{s->dc});
+    else
+        launch_diagnostics(g, st, s->XP, s->v, s->skeys, s->perm, s->cstart, s->cend,
+                                            s->VX, n, ManyScenes{s->d_consts, s->sid_sorted});
     PBF_CUDA(s, cudaGetLastError());
     std::vector<float4> h(n);
     PBF_CUDA(s, cudaMemcpyAsync(h.data(), s->VX, sizeof(float4) * n, cudaMemcpyDeviceToHost, st));
@@ -757,7 +866,7 @@ pbf_status pbf_find_cells(const uint32_t* sorted_keys, uint32_t n, uint32_t num_
     if (e == cudaSuccess) e = cudaMemsetAsync(end, 0xFF, sizeof(int32_t) * (size_t)num_cells, st);
     if (e == cudaSuccess && n > 0) {
         k_find_cells<<<grid_for(n), kBlock, 0, st>>>(sorted_keys, nullptr, nullptr, nullptr, n,
-                                                     num_cells, start, end, bad);
+                                                     num_cells, start, end, bad, nullptr, nullptr);
         e = cudaGetLastError();
     }
     uint32_t hbad = 0;

@@ -35,6 +35,7 @@ struct DevConsts {
     uint32_t Gi[3];
     uint32_t GxGz;    // hash weight of y (src/SPH.cpp:31)
     uint32_t ncells;
+    uint32_t cell_base;  // first global cell index of this scene (0 for a single scene)
     uint32_t ext_force;
     // neighbour lists (a tuning choice: results are identical with or without)
     uint32_t use_lists;
@@ -112,8 +113,21 @@ __device__ __forceinline__ uint32_t cell_key(float3 q, const DevConsts& c) {
     uint32_t cx = cell_coord(q.x, c.G[0], c.Gi[0]);
     uint32_t cy = cell_coord(q.y, c.G[1], c.Gi[1]);
     uint32_t cz = cell_coord(q.z, c.G[2], c.Gi[2]);
-    return cx + cy * c.GxGz + cz * c.Gi[0];
+    return c.cell_base + cx + cy * c.GxGz + cz * c.Gi[0];
 }
+
+// Where a kernel finds the constants of particle i.  One scene: the kernel
+// parameter itself (constant bank, no load).  Several scenes: the particle's
+// scene id indexes a device table of per-scene constants.
+struct OneScene {
+    DevConsts c;
+    __device__ __forceinline__ const DevConsts& at(uint32_t) const { return c; }
+};
+struct ManyScenes {
+    const DevConsts* __restrict__ cs;
+    const uint32_t* __restrict__ sid;  // scene of each particle (id or sorted order)
+    __device__ __forceinline__ const DevConsts& at(uint32_t i) const { return cs[__ldg(sid + i)]; }
+};
 
 __device__ __forceinline__ bool finite3(float3 a) {
     return isfinite(a.x) && isfinite(a.y) && isfinite(a.z);

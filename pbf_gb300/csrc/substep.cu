@@ -31,8 +31,9 @@ __device__ __forceinline__ void runs_of(uint32_t key, const DevConsts& c,
                                         const int32_t* __restrict__ cstart,
                                         const int32_t* __restrict__ cend, Runs& r) {
     const uint32_t Gx = c.Gi[0], Gy = c.Gi[1], Gz = c.Gi[2];
-    const int cx = (int)(key % Gx);
-    const uint32_t rem = key / Gx;
+    const uint32_t local = key - c.cell_base;
+    const int cx = (int)(local % Gx);
+    const uint32_t rem = local / Gx;
     const int cz = (int)(rem % Gz);
     const int cy = (int)(rem / Gz);
     const int xlo = cx > 0 ? cx - 1 : 0;
@@ -42,7 +43,7 @@ __device__ __forceinline__ void runs_of(uint32_t key, const DevConsts& c,
         const int ny = cy + (o / 3) - 1, nz = cz + (o % 3) - 1;
         int32_t first = -1, last = -1;
         if (ny >= 0 && ny < (int)Gy && nz >= 0 && nz < (int)Gz) {
-            const uint32_t base = (uint32_t)ny * c.GxGz + (uint32_t)nz * Gx;
+            const uint32_t base = c.cell_base + (uint32_t)ny * c.GxGz + (uint32_t)nz * Gx;
             for (int xx = xlo; xx <= xhi; ++xx) {
                 const int32_t s = __ldg(cstart + base + (uint32_t)xx);
                 if (s != -1) {
@@ -59,11 +60,13 @@ __device__ __forceinline__ void runs_of(uint32_t key, const DevConsts& c,
 }  // namespace
 
 // predictpos.glsl:18-38 fused with the cell key of GetHash (counting.glsl:53-57).
+template <class CP>
 __global__ void __launch_bounds__(kBlock)
 k_predict(const float4* __restrict__ x, const float4* __restrict__ v, float4* __restrict__ xstar,
-          uint32_t* __restrict__ keys, uint32_t n, DevConsts c, uint32_t* status) {
+          uint32_t* __restrict__ keys, uint32_t n, CP cp, uint32_t* status) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const auto& c = cp.at(i);
     const float4 q = x[i];
     const float4 w = v[i];
     float wz = w.z;
@@ -77,11 +80,13 @@ k_predict(const float4* __restrict__ x, const float4* __restrict__ v, float4* __
 }
 
 // Cell keys of the current positions (no prediction), for diagnostics.
+template <class CP>
 __global__ void __launch_bounds__(kBlock)
 k_keys_of(const float4* __restrict__ x, float4* __restrict__ xstar, uint32_t* __restrict__ keys,
-          uint32_t n, DevConsts c) {
+          uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const auto& c = cp.at(i);
     const float4 q = x[i];
     xstar[i] = make_float4(q.x, q.y, q.z, 0.0f);
     keys[i] = cell_key(xyz(q), c);
@@ -104,11 +109,13 @@ k_unmark_cells(const uint32_t* __restrict__ prev_sorted, uint32_t n, uint32_t nc
 __global__ void __launch_bounds__(kBlock)
 k_find_cells(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
              const float4* __restrict__ xstar, float4* __restrict__ P0, uint32_t n, uint32_t ncells,
-             int32_t* __restrict__ cstart, int32_t* __restrict__ cend, uint32_t* bad) {
+             int32_t* __restrict__ cstart, int32_t* __restrict__ cend, uint32_t* bad,
+             const uint32_t* __restrict__ sid, uint32_t* __restrict__ sid_sorted) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t k = skeys[i];
     if (P0) P0[i] = __ldg(xstar + perm[i]);
+    if (sid_sorted) sid_sorted[i] = __ldg(sid + perm[i]);
     if (k >= ncells) {
         atomicOr(bad, 1u);
         return;
@@ -155,7 +162,7 @@ __device__ __forceinline__ void visit_list(uint32_t i, int32_t cnt, const NbrLis
 // predicted ones?  NaN anywhere makes the answer false.
 __device__ __forceinline__ bool list_usable(const DevConsts& c, const NbrLists& nl, int32_t cnt,
                                             float3 pi, float3 xi, int dmax_slot) {
-    if (!c.use_lists || cnt < 0) return false;
+    if (!c.use_lists || cnt < 0 || dmax_slot < -1) return false;  // -2: no lists built
     const float3 dd = make_float3(pi.x - xi.x, pi.y - xi.y, pi.z - xi.z);
     const float di = sqrtf(dd.x * dd.x + dd.y * dd.y + dd.z * dd.z) * 1.0001f;
     const float dmax = dmax_slot < 0 ? 0.0f : __uint_as_float(nl.guard[dmax_slot]) * 1.0001f;
@@ -211,14 +218,16 @@ constexpr int kSweepBlocksPerSM = 8;
 // positions XP: a full stencil scan that also records, in visit order, every
 // candidate within h + skin (the neighbour list of the later sweeps) and the
 // largest coordinate magnitude (for the guard's rounding margin).
+template <class CP>
 __global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
 k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys,
                const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
-               float4* __restrict__ L, NbrLists nl, uint32_t n, DevConsts c) {
+               float4* __restrict__ L, NbrLists nl, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < n;
     float3 pi = make_float3(0.0f, 0.0f, 0.0f);
     if (live) {
+        const auto& c = cp.at(i);
         pi = xyz(XP[i]);
         LambdaAcc a{0.0f, 0.0f, make_float3(0.0f, 0.0f, 0.0f)};
         int32_t cnt = 0;
@@ -241,13 +250,15 @@ k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys
 
 // calclambda.glsl:66-102 at positions P (iterations after the first).
 // dmax_slot: guard slot holding the largest displacement of P from XP.
+template <class CP>
 __global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
 k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
          const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cstart,
          const int32_t* __restrict__ cend, float4* __restrict__ L, NbrLists nl, int dmax_slot,
-         uint32_t n, DevConsts c) {
+         uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const auto& c = cp.at(i);
     const float3 pi = xyz(P[i]);
     LambdaAcc a{0.0f, 0.0f, make_float3(0.0f, 0.0f, 0.0f)};
     auto body = [&](uint32_t j) {
@@ -264,15 +275,17 @@ k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
 
 // updatepos.glsl:42-104.  Reads L = (p, lambda), writes clamped positions Pn
 // and the largest displacement of Pn from XP into guard slot `out_slot`.
+template <class CP>
 __global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
 k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
           const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cstart,
           const int32_t* __restrict__ cend, float4* __restrict__ Pn, NbrLists nl, int dmax_slot,
-          int out_slot, uint32_t n, DevConsts c, uint32_t* status) {
+          int out_slot, uint32_t n, CP cp, uint32_t* status) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < n;
     float disp = 0.0f;
     if (live) {
+        const auto& c = cp.at(i);
         const float4 Li = L[i];
         const float3 pi = xyz(Li);
         const float li = Li.w;
@@ -318,11 +331,13 @@ k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
 // update.glsl:16-28: v = (x* - x_old) / dt, x = x*, scattered back to id order.
 // VS receives the committed velocity in sorted order; when `v_out` is set the
 // velocity is also stored in id order (vorticity confinement disabled).
+template <class CP>
 __global__ void __launch_bounds__(kBlock)
 k_commit(const float4* __restrict__ P, const uint32_t* __restrict__ perm, float4* __restrict__ x,
-         float4* __restrict__ VS, float4* __restrict__ v_out, uint32_t n, DevConsts c) {
+         float4* __restrict__ VS, float4* __restrict__ v_out, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const auto& c = cp.at(i);
     const uint32_t id = perm[i];
     const float4 q = P[i];
     const float4 xo = x[id];
@@ -335,14 +350,16 @@ k_commit(const float4* __restrict__ P, const uint32_t* __restrict__ perm, float4
 
 // vorticity.glsl:34-60: XSPH velocity and the vorticity vector, Jacobi
 // (every read sees the committed velocities).
+template <class CP>
 __global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
 k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
               const float4* __restrict__ VS, const uint32_t* __restrict__ skeys,
               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
               float4* __restrict__ VX, float4* __restrict__ OM, float4* __restrict__ Q,
-              NbrLists nl, int dmax_slot, uint32_t n, DevConsts c) {
+              NbrLists nl, int dmax_slot, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const auto& c = cp.at(i);
     const float3 pi = xyz(P[i]);
     const float3 vi = xyz(VS[i]);
     float3 acc = make_float3(0.0f, 0.0f, 0.0f), w = make_float3(0.0f, 0.0f, 0.0f);
@@ -371,14 +388,16 @@ k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
 
 // vorticity.glsl:65-85: confinement from the gradient of |vorticity|; writes
 // the final velocity in id order.
+template <class CP>
 __global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
 k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ XP,
               const float4* __restrict__ VX, const float4* __restrict__ OM,
               const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
-              float4* __restrict__ v, NbrLists nl, int dmax_slot, uint32_t n, DevConsts c) {
+              float4* __restrict__ v, NbrLists nl, int dmax_slot, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const auto& c = cp.at(i);
     const float3 pi = xyz(Q[i]);
     float3 eta = make_float3(0.0f, 0.0f, 0.0f);
     auto pos = [&](uint32_t j) { return xyz(__ldg(Q + j)); };
@@ -404,13 +423,15 @@ k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ XP,
 
 // Per-particle density error |rho/rho0 - 1| (self excluded) and kinetic
 // energy of the state sorted into P (positions) with velocities v (id order).
+template <class CP>
 __global__ void __launch_bounds__(kBlock)
 k_diagnostics(const float4* __restrict__ P, const float4* __restrict__ v,
               const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
-              float4* __restrict__ out, uint32_t n, DevConsts c) {
+              float4* __restrict__ out, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const auto& c = cp.at(i);
     Runs r;
     runs_of(skeys[i], c, cstart, cend, r);
     const float3 pi = xyz(P[i]);
@@ -430,5 +451,95 @@ k_diagnostics(const float4* __restrict__ P, const float4* __restrict__ v,
     out[i] = make_float4(fabsf(ffma(rho, c.oorho, -1.0f)),
                          0.5f * (w.x * w.x + w.y * w.y + w.z * w.z), (float)cand, 0.0f);
 }
+
+// Host-side launchers: the template kernels are launched from this file
+// (their host stubs are not visible to other translation units).
+template <class CP>
+void launch_predict(unsigned g, cudaStream_t st, const float4* x, const float4* v, float4* xstar,
+                    uint32_t* keys, uint32_t n, CP cp, uint32_t* status) {
+    k_predict<CP><<<g, kBlock, 0, st>>>(x, v, xstar, keys, n, cp, status);
+}
+template <class CP>
+void launch_keys_of(unsigned g, cudaStream_t st, const float4* x, float4* xstar, uint32_t* keys,
+                    uint32_t n, CP cp) {
+    k_keys_of<CP><<<g, kBlock, 0, st>>>(x, xstar, keys, n, cp);
+}
+template <class CP>
+void launch_lambda_build(unsigned g, cudaStream_t st, const float4* XP, const uint32_t* skeys,
+                         const int32_t* cstart, const int32_t* cend, float4* L, NbrLists nl,
+                         uint32_t n, CP cp) {
+    k_lambda_build<CP><<<g, kBlock, 0, st>>>(XP, skeys, cstart, cend, L, nl, n, cp);
+}
+template <class CP>
+void launch_lambda(unsigned g, cudaStream_t st, const float4* P, const float4* XP,
+                   const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* L,
+                   NbrLists nl, int dmax_slot, uint32_t n, CP cp) {
+    k_lambda<CP><<<g, kBlock, 0, st>>>(P, XP, skeys, cstart, cend, L, nl, dmax_slot, n, cp);
+}
+template <class CP>
+void launch_delta_p(unsigned g, cudaStream_t st, const float4* L, const float4* XP,
+                    const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* Pn,
+                    NbrLists nl, int dmax_slot, int out_slot, uint32_t n, CP cp, uint32_t* status) {
+    k_delta_p<CP><<<g, kBlock, 0, st>>>(L, XP, skeys, cstart, cend, Pn, nl, dmax_slot, out_slot, n,
+                                        cp, status);
+}
+template <class CP>
+void launch_commit(unsigned g, cudaStream_t st, const float4* P, const uint32_t* perm, float4* x,
+                   float4* VS, float4* v_out, uint32_t n, CP cp) {
+    k_commit<CP><<<g, kBlock, 0, st>>>(P, perm, x, VS, v_out, n, cp);
+}
+template <class CP>
+void launch_vorticity_a(unsigned g, cudaStream_t st, const float4* P, const float4* XP,
+                        const float4* VS, const uint32_t* skeys, const int32_t* cstart,
+                        const int32_t* cend, float4* VX, float4* OM, float4* Q, NbrLists nl,
+                        int dmax_slot, uint32_t n, CP cp) {
+    k_vorticity_a<CP><<<g, kBlock, 0, st>>>(P, XP, VS, skeys, cstart, cend, VX, OM, Q, nl,
+                                            dmax_slot, n, cp);
+}
+template <class CP>
+void launch_vorticity_b(unsigned g, cudaStream_t st, const float4* Q, const float4* XP,
+                        const float4* VX, const float4* OM, const uint32_t* skeys,
+                        const uint32_t* perm, const int32_t* cstart, const int32_t* cend,
+                        float4* v, NbrLists nl, int dmax_slot, uint32_t n, CP cp) {
+    k_vorticity_b<CP><<<g, kBlock, 0, st>>>(Q, XP, VX, OM, skeys, perm, cstart, cend, v, nl,
+                                            dmax_slot, n, cp);
+}
+template <class CP>
+void launch_diagnostics(unsigned g, cudaStream_t st, const float4* P, const float4* v,
+                        const uint32_t* skeys, const uint32_t* perm, const int32_t* cstart,
+                        const int32_t* cend, float4* out, uint32_t n, CP cp) {
+    k_diagnostics<CP><<<g, kBlock, 0, st>>>(P, v, skeys, perm, cstart, cend, out, n, cp);
+}
+
+#define PBF_INSTANTIATE(CP)                                                                     \
+    template void launch_predict<CP>(unsigned, cudaStream_t, const float4*, const float4*,      \
+                                     float4*, uint32_t*, uint32_t, CP, uint32_t*);              \
+    template void launch_keys_of<CP>(unsigned, cudaStream_t, const float4*, float4*, uint32_t*, \
+                                     uint32_t, CP);                                             \
+    template void launch_lambda_build<CP>(unsigned, cudaStream_t, const float4*, const uint32_t*, \
+                                          const int32_t*, const int32_t*, float4*, NbrLists,    \
+                                          uint32_t, CP);                                        \
+    template void launch_lambda<CP>(unsigned, cudaStream_t, const float4*, const float4*,       \
+                                    const uint32_t*, const int32_t*, const int32_t*, float4*,   \
+                                    NbrLists, int, uint32_t, CP);                               \
+    template void launch_delta_p<CP>(unsigned, cudaStream_t, const float4*, const float4*,      \
+                                     const uint32_t*, const int32_t*, const int32_t*, float4*,  \
+                                     NbrLists, int, int, uint32_t, CP, uint32_t*);              \
+    template void launch_commit<CP>(unsigned, cudaStream_t, const float4*, const uint32_t*,     \
+                                    float4*, float4*, float4*, uint32_t, CP);                   \
+    template void launch_vorticity_a<CP>(unsigned, cudaStream_t, const float4*, const float4*,  \
+                                         const float4*, const uint32_t*, const int32_t*,        \
+                                         const int32_t*, float4*, float4*, float4*, NbrLists,   \
+                                         int, uint32_t, CP);                                    \
+    template void launch_vorticity_b<CP>(unsigned, cudaStream_t, const float4*, const float4*,  \
+                                         const float4*, const float4*, const uint32_t*,         \
+                                         const uint32_t*, const int32_t*, const int32_t*,       \
+                                         float4*, NbrLists, int, uint32_t, CP);                 \
+    template void launch_diagnostics<CP>(unsigned, cudaStream_t, const float4*, const float4*,  \
+                                         const uint32_t*, const uint32_t*, const int32_t*,      \
+                                         const int32_t*, float4*, uint32_t, CP);
+
+PBF_INSTANTIATE(OneScene)
+PBF_INSTANTIATE(ManyScenes)
 
 }  // namespace pbf

@@ -1,50 +1,55 @@
-// substep.cuh — stage kernels of one PBF substep (definitions in substep.cu).
+// substep.cuh — stage kernels of one PBF substep (definitions and the
+// explicit instantiations for OneScene / ManyScenes in substep.cu).
 #pragma once
 
 #include "common.cuh"
 
 namespace pbf {
 
-__global__ void k_predict(const float4* __restrict__ x, const float4* __restrict__ v,
-                          float4* __restrict__ xstar, uint32_t* __restrict__ keys, uint32_t n,
-                          DevConsts c, uint32_t* status);
-__global__ void k_keys_of(const float4* __restrict__ x, float4* __restrict__ xstar,
-                          uint32_t* __restrict__ keys, uint32_t n, DevConsts c);
 __global__ void k_unmark_cells(const uint32_t* __restrict__ prev_sorted, uint32_t n,
                                uint32_t ncells, int32_t* __restrict__ cstart);
 __global__ void k_find_cells(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
                              const float4* __restrict__ xstar, float4* __restrict__ P0, uint32_t n,
                              uint32_t ncells, int32_t* __restrict__ cstart,
-                             int32_t* __restrict__ cend, uint32_t* bad);
-__global__ void k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys,
-                               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
-                               float4* __restrict__ L, NbrLists nl, uint32_t n, DevConsts c);
-__global__ void k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
-                         const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cstart,
-                         const int32_t* __restrict__ cend, float4* __restrict__ L, NbrLists nl,
-                         int dmax_slot, uint32_t n, DevConsts c);
-__global__ void k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
-                          const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cstart,
-                          const int32_t* __restrict__ cend, float4* __restrict__ Pn, NbrLists nl,
-                          int dmax_slot, int out_slot, uint32_t n, DevConsts c, uint32_t* status);
-__global__ void k_commit(const float4* __restrict__ P, const uint32_t* __restrict__ perm,
-                         float4* __restrict__ x, float4* __restrict__ VS,
-                         float4* __restrict__ v_out, uint32_t n, DevConsts c);
-__global__ void k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
-                              const float4* __restrict__ VS, const uint32_t* __restrict__ skeys,
-                              const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
-                              float4* __restrict__ VX, float4* __restrict__ OM,
-                              float4* __restrict__ Q, NbrLists nl, int dmax_slot, uint32_t n,
-                              DevConsts c);
-__global__ void k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ XP,
-                              const float4* __restrict__ VX, const float4* __restrict__ OM,
-                              const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
-                              const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
-                              float4* __restrict__ v, NbrLists nl, int dmax_slot, uint32_t n,
-                              DevConsts c);
-__global__ void k_diagnostics(const float4* __restrict__ P, const float4* __restrict__ v,
-                              const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
-                              const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
-                              float4* __restrict__ out, uint32_t n, DevConsts c);
+                             int32_t* __restrict__ cend, uint32_t* bad,
+                             const uint32_t* __restrict__ sid, uint32_t* __restrict__ sid_sorted);
+
+// Host launchers of the templated stage kernels (explicitly instantiated for
+// OneScene and ManyScenes in substep.cu).
+template <class CP>
+void launch_predict(unsigned g, cudaStream_t st, const float4* x, const float4* v, float4* xstar,
+                    uint32_t* keys, uint32_t n, CP cp, uint32_t* status);
+template <class CP>
+void launch_keys_of(unsigned g, cudaStream_t st, const float4* x, float4* xstar, uint32_t* keys,
+                    uint32_t n, CP cp);
+template <class CP>
+void launch_lambda_build(unsigned g, cudaStream_t st, const float4* XP, const uint32_t* skeys,
+                         const int32_t* cstart, const int32_t* cend, float4* L, NbrLists nl,
+                         uint32_t n, CP cp);
+template <class CP>
+void launch_lambda(unsigned g, cudaStream_t st, const float4* P, const float4* XP,
+                   const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* L,
+                   NbrLists nl, int dmax_slot, uint32_t n, CP cp);
+template <class CP>
+void launch_delta_p(unsigned g, cudaStream_t st, const float4* L, const float4* XP,
+                    const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* Pn,
+                    NbrLists nl, int dmax_slot, int out_slot, uint32_t n, CP cp, uint32_t* status);
+template <class CP>
+void launch_commit(unsigned g, cudaStream_t st, const float4* P, const uint32_t* perm, float4* x,
+                   float4* VS, float4* v_out, uint32_t n, CP cp);
+template <class CP>
+void launch_vorticity_a(unsigned g, cudaStream_t st, const float4* P, const float4* XP,
+                        const float4* VS, const uint32_t* skeys, const int32_t* cstart,
+                        const int32_t* cend, float4* VX, float4* OM, float4* Q, NbrLists nl,
+                        int dmax_slot, uint32_t n, CP cp);
+template <class CP>
+void launch_vorticity_b(unsigned g, cudaStream_t st, const float4* Q, const float4* XP,
+                        const float4* VX, const float4* OM, const uint32_t* skeys,
+                        const uint32_t* perm, const int32_t* cstart, const int32_t* cend,
+                        float4* v, NbrLists nl, int dmax_slot, uint32_t n, CP cp);
+template <class CP>
+void launch_diagnostics(unsigned g, cudaStream_t st, const float4* P, const float4* v,
+                        const uint32_t* skeys, const uint32_t* perm, const int32_t* cstart,
+                        const int32_t* cend, float4* out, uint32_t n, CP cp);
 
 }  // namespace pbf

@@ -129,18 +129,38 @@ def diff_32k(seed_a: int = 1, seed_b: int = 2):
 
 def batch_scene_specs(num_scenes: int = 256, seed: int = 7, nmin: int = 4096, nmax: int = 65536,
                       box_min: int = 32, box_max: int = 96):
-    """Per-scene (lattice, box) of the batched workload: block dimensions drawn
-    so counts are uniform-integer in [nmin, nmax], box sides uniform in
-    [box_min, box_max] cells, the block fitting inside its box."""
+    """Per-scene (lattice, box) of a batched workload: a target count drawn
+    uniform-integer in [nmin, nmax], box sides uniform in [box_min, box_max]
+    cells, and block dimensions (x = z near the cube root, y the rest) whose
+    product is the target rounded to the block's shape, the block fitting
+    inside its box at spacing 0.5."""
     rng = np.random.Generator(np.random.PCG64(seed))
     specs = []
     for _ in range(num_scenes):
         target = int(rng.integers(nmin, nmax + 1))
         box = [int(rng.integers(box_min, box_max + 1)) for _ in range(3)]
-        # block dims: x, z up to the box at spacing 0.5, y the rest
         cap = [max(1, int((b - 1) / SPACING)) for b in box]
-        bx = min(cap[0], max(1, int(round(target ** (1 / 3)))))
-        bz = min(cap[2], max(1, int(round(target ** (1 / 3)))))
+        side = max(1, int(round(target ** (1 / 3))))
+        bx = min(cap[0], side)
+        bz = min(cap[2], side)
         by = max(1, min(cap[1], int(round(target / (bx * bz)))))
         specs.append({"lattice": [bx, by, bz], "box": box})
     return specs
+
+
+def batch_scenes(num_scenes: int = 256, seed: int = 7, iterations: int = 4, substeps: int = 100,
+                 nmin: int = 4096, nmax: int = 65536, box_min: int = 32, box_max: int = 96,
+                 vel_uniform: float = 0.5) -> list[Scene]:
+    """The batched dam breaks: per scene a seeded block (jitter U(-0.01h, 0.01h),
+    velocities U(-0.5, 0.5)) in its own box, the shared constants above."""
+    out = []
+    for k, spec in enumerate(batch_scene_specs(num_scenes, seed, nmin, nmax, box_min, box_max)):
+        x4, v4 = block(spec["lattice"], seed=seed * 100003 + k, vel_uniform=vel_uniform)
+        out.append(Scene(f"batch{k}", dam_params(spec["box"], iterations), x4, v4, substeps,
+                         {**spec, "seed": seed * 100003 + k}))
+    return out
+
+
+def concat_state(scenes_: list[Scene]):
+    return (np.ascontiguousarray(np.concatenate([s.x4 for s in scenes_])),
+            np.ascontiguousarray(np.concatenate([s.v4 for s in scenes_])))

@@ -266,7 +266,7 @@ class SPH:
         return kb, sk, pm
 
     def get_cells(self) -> tuple[np.ndarray, np.ndarray]:
-        nc = int(np.prod([int(g) for g in self._params.grid]))
+        nc = int(self._lib.pbf_num_cells(self._h))
         st = np.empty(nc, np.int32)
         en = np.empty(nc, np.int32)
         check(self._lib.pbf_get_cells(self._h, st.ctypes.data, en.ctypes.data), self._h)
@@ -284,4 +284,49 @@ class SPH:
         return {name: getattr(d, name) for name, _ in Diagnostics._fields_}
 
 
-__all__ = ["SPH", "default_params", "PbfError"]
+class SPHBatch(SPH):
+    """Several independent scenes in one handle (pbf_create_batch).
+
+    State arrays are the scenes' float4 arrays concatenated in scene order;
+    every stage runs as one launch over all scenes, and each scene steps
+    bit-identically to the same scene in its own :class:`SPH`.
+    """
+
+    def __init__(self, scene_params, scene_counts):
+        self._lib = load()
+        ps = list(scene_params)
+        counts = [int(c) for c in scene_counts]
+        if len(ps) != len(counts) or not ps:
+            raise ValueError("one particle count per scene")
+        arr = (Params * len(ps))(*[p.copy() for p in ps])
+        cnt = (C.c_uint32 * len(counts))(*counts)
+        h = C.c_void_p()
+        check(self._lib.pbf_create_batch(arr, cnt, len(ps), C.byref(h)))
+        self._h = h
+        self._n = sum(counts)
+        self._params = ps[0].copy()
+        self._scene_params = [p.copy() for p in ps]
+        self._counts = counts
+        self._offsets = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+
+    @property
+    def num_scenes(self) -> int:
+        return len(self._counts)
+
+    def scene_slice(self, k: int) -> slice:
+        return slice(int(self._offsets[k]), int(self._offsets[k + 1]))
+
+    def scene_params(self, k: int) -> Params:
+        return self._scene_params[k].copy()
+
+    def set_scene_params(self, k: int, p: Params) -> None:
+        check(self._lib.pbf_set_scene_params(self._h, int(k), C.byref(p)), self._h)
+        self._scene_params[k] = p.copy()
+        if k == 0:
+            self._params = p.copy()
+
+    def set_params(self, p: Params) -> None:
+        raise PbfError(1, "a batch takes set_scene_params")
+
+
+__all__ = ["SPH", "SPHBatch", "default_params", "PbfError"]
