@@ -62,6 +62,9 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=0, help="0: min(steps, 50)")
     ap.add_argument("--no-stable", action="store_true", help="skip the epsilon = 5 full run")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-scene comparison")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the backward/forward ratio")
+    ap.add_argument("--recovery", action="store_true",
+                    help="also run the 64-scene parameter recovery (about a minute)")
     return ap.parse_args()
 
 
@@ -201,6 +204,141 @@ def batched_vs_plain(stream, num_scenes: int = 256, substeps: int = 100):
             "plain_scenes_per_s": num_scenes / (tp * 1e-3), "speedup": tp / tb,
             "batched_particle_iters_per_s": n * it * substeps / (tb * 1e-3),
             "bit_identical_sampled_scenes": bool(same)}
+
+
+def adjoint_ratio(stream, substeps: int = 64, every: int = 8):
+    """Backward / forward time of the differentiable scene: 32,768 particles
+    (32^3 lattice) in a 64^3 box, velocities N(0, 0.25^2) from seed A, 64
+    substeps x 4 iterations; loss = mean squared distance of the final
+    positions to those of a run from seed-B velocities.  Forward = the
+    recorded run (checkpoint every 8 substeps); backward = recomputing each
+    8-substep segment with its tape plus the adjoint kernels."""
+    import torch
+    import numpy as np
+    import pbf_gb300 as pg
+    from pbf_gb300 import scenes
+    a, b = scenes.diff_32k()
+    n = a.n
+    tgt = pg.SPH(n, tuple(b.params.grid), b.params)
+    tgt.set_state(b.x4, b.v4)
+    tgt.step(substeps)
+    target = tgt.positions()
+    tgt.close()
+    sim = pg.SPH(n, tuple(a.params.grid), a.params)
+    sim.set_stream(stream.cuda_stream)
+    sim.set_state(a.x4, a.v4)
+    sim.forward_record(substeps, every)  # warm-up (graph capture, tape allocation)
+    x = sim.positions()
+    w = (2.0 / n) * (x - target)
+    w[:, 3] = 0
+    sim.backward(w, None)
+    fwd, bwd = [], []
+    for _ in range(3):
+        sim.set_state(a.x4, a.v4)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim.forward_record(substeps, every)
+        sim.synchronize()
+        t1 = time.perf_counter()
+        x = sim.positions()
+        w = (2.0 / n) * (x - target)
+        w[:, 3] = 0
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        dx0, dv0, g = sim.backward(w, None)
+        t3 = time.perf_counter()
+        fwd.append(t1 - t0)
+        bwd.append(t3 - t2)
+    loss = float(np.mean(np.sum((x[:, :3] - target[:, :3]) ** 2, axis=1)))
+    f, bk = min(fwd), min(bwd)
+    sim.close()
+    return {"particles": n, "substeps": substeps, "iterations": a.params.num_solver_iterations,
+            "checkpoint_every": every, "forward_ms": f * 1e3, "backward_ms": bk * 1e3,
+            "bwd_fwd_ratio": bk / f, "loss": loss,
+            "grad_norm_v0": float(np.linalg.norm(dv0[:, :3])),
+            "grad_params": dict(zip(pg.SPH.PARAM_NAMES, [float(v) for v in g[0]])),
+            "note": "wall-clock per call, host synchronised; backward includes the "
+                    "recomputation of every checkpoint segment"}
+
+
+def recovery(stream, num_scenes: int = 64, substeps: int = 32, steps: int = 50, seed: int = 11,
+             epsilon: float = 0.01):
+    """Batched differentiable parameter recovery: 64 scenes (8,192-32,768
+    particles, boxes 48-80 cells, 32 substeps x 4 iterations).  Hidden per-scene
+    XSPH c ~ U(0.005, 0.02) and vorticity epsilon ~ U(0, 0.001) generate the
+    target final positions; starting from c = 0.01, epsilon = 0.0005, `steps`
+    Adam steps on the per-scene mean squared distance, each one batched
+    forward_record + backward (checkpoint every 8 substeps)."""
+    import numpy as np
+    import pbf_gb300 as pg
+    from pbf_gb300 import scenes
+    rng = np.random.default_rng(seed)
+    scs = scenes.batch_scenes(num_scenes, seed=seed, iterations=4, substeps=substeps, nmin=8192,
+                              nmax=32768, box_min=48, box_max=80)
+    for s_ in scs:
+        s_.params.epsilon = epsilon
+    hidden = np.stack([rng.uniform(0.005, 0.02, num_scenes), rng.uniform(0.0, 0.001, num_scenes)], 1)
+    x4, v4 = scenes.concat_state(scs)
+    batch = pg.SPHBatch([s.params for s in scs], [s.n for s in scs])
+    batch.set_stream(stream.cuda_stream)
+
+    def set_theta(th):
+        for k in range(num_scenes):
+            p = batch.scene_params(k)
+            p.xsph_viscosity_c = float(np.float32(th[k, 0]))
+            p.vorticity_epsilon = float(np.float32(th[k, 1]))
+            batch.set_scene_params(k, p)
+
+    set_theta(hidden)
+    batch.set_state(x4, v4)
+    batch.step(substeps)
+    target = batch.positions()
+    theta = np.tile([0.01, 0.0005], (num_scenes, 1))
+    scale = np.array([0.015, 0.001])
+    m = np.zeros_like(theta)
+    vv = np.zeros_like(theta)
+    lr, b1, b2 = 0.05, 0.9, 0.999
+    counts = np.array([s.n for s in scs], np.float64)
+    sl = [batch.scene_slice(k) for k in range(num_scenes)]
+    times, losses = [], []
+    nonfinite = 0
+    for it in range(steps):
+        t0 = time.perf_counter()
+        set_theta(theta)
+        batch.set_state(x4, v4)
+        batch.forward_record(substeps, 8)
+        x = batch.positions()
+        w = np.zeros_like(x)
+        loss = np.zeros(num_scenes)
+        for k in range(num_scenes):
+            d = x[sl[k], :3] - target[sl[k], :3]
+            loss[k] = float(np.mean(np.sum(d * d, axis=1)))
+            w[sl[k], :3] = (2.0 / counts[k]) * d
+        _, _, g = batch.backward(w, None)
+        times.append(time.perf_counter() - t0)
+        losses.append(float(loss.mean()))
+        grad = g[:, [2, 3]] * scale  # d loss / d (theta / scale)
+        bad = ~np.all(np.isfinite(grad), axis=1)
+        nonfinite += int(bad.sum())
+        grad[bad] = 0.0
+        m = b1 * m + (1 - b1) * grad
+        vv = b2 * vv + (1 - b2) * grad * grad
+        mh = m / (1 - b1 ** (it + 1))
+        vh = vv / (1 - b2 ** (it + 1))
+        step = lr * mh / (np.sqrt(vh) + 1e-30)
+        theta = np.clip(theta - step * scale, [0.0, 0.0], [0.05, 0.005])
+    err0 = np.abs(np.tile([0.01, 0.0005], (num_scenes, 1)) - hidden) / scale
+    err = np.abs(theta - hidden) / scale
+    batch.close()
+    return {"scenes": num_scenes, "particles": int(x4.shape[0]), "substeps": substeps,
+            "gd_steps": steps, "ms_per_gd_step": 1e3 * float(np.median(times)),
+            "loss_first": losses[0], "loss_last": losses[-1],
+            "param_error_start": {"xsph_c": float(err0[:, 0].mean()),
+                                  "vorticity_epsilon": float(err0[:, 1].mean())},
+            "param_error_end": {"xsph_c": float(err[:, 0].mean()),
+                                "vorticity_epsilon": float(err[:, 1].mean())},
+            "epsilon": epsilon, "scene_gradients_nonfinite": nonfinite,
+            "note": "errors are mean |theta - hidden| / range (0.015 for c, 0.001 for eps_v)"}
 
 
 def cpu_baseline(scene, substeps: int):
@@ -385,6 +523,15 @@ def main():
                                           "(src/SPH.cpp:138), full run"}
         sim.set_params(scene.params)
 
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = adjoint_ratio(stream)
+
+    recov = None
+    if args.recovery:
+        recov = {"workload_epsilon_0.01": recovery(stream),
+                 "reference_default_epsilon_5": recovery(stream, epsilon=5.0)}
+
     batched = None
     if not args.no_batched:
         sim.close()
@@ -419,6 +566,8 @@ def main():
             "gpu_launches": launches,
             "stable_500": stable,
             "batched_256": batched,
+            "adjoint_32k": adjoint,
+            "recovery_64": recov,
             "clocks": clk,
             "cpu_baseline": cpu,
         }

@@ -269,6 +269,39 @@ pbf_status pbf_radix_sort_noalloc(const uint32_t* keys_in, uint32_t* keys_out, u
 pbf_status pbf_find_cells(const uint32_t* sorted_keys, uint32_t n, uint32_t num_cells,
                           int32_t* start, int32_t* end, void* stream);
 
+/* ---- differentiation (no reference counterpart) ------------------------------ */
+
+/* Gradient of a scalar loss with respect to the scalar parameters; one per
+ * scene (an array of pbf_num_scenes() entries). */
+typedef struct pbf_param_grads {
+    double epsilon;                /* CFM relaxation epsilon */
+    double tensile_instability_k;  /* s_corr k */
+    double xsph_viscosity_c;       /* XSPH c */
+    double vorticity_epsilon;      /* vorticity confinement epsilon */
+} pbf_param_grads;
+
+/* Runs `substeps` substeps from the current state like pbf_step and keeps
+ * what pbf_backward needs: the state every `checkpoint_every` substeps (the
+ * substeps in between are recomputed during the backward pass) and the final
+ * state.  Parameters must not change until pbf_backward; pbf_set_params and
+ * pbf_set_scene_params drop the recording. */
+pbf_status pbf_forward_record(pbf_sim* sim, uint32_t substeps, uint32_t checkpoint_every);
+
+/* Reverse-mode gradient of a loss L(x_final, v_final) through the recorded
+ * substeps: dL_dx4 / dL_dv4 (float4 per particle, id order; NULL = zero) are
+ * the loss gradients at the end of the run; dL_dx0_4 / dL_dv0_4 receive the
+ * gradients with respect to the state at the start (either may be NULL), and
+ * grads (NULL or one entry per scene) those with respect to the scalar
+ * parameters.  The sort permutation and neighbour candidates are frozen from
+ * the forward pass (piecewise constant); the wall clamp contributes its
+ * subgradient.  Hand-written adjoint kernels, FP32, deterministic.  Leaves the
+ * state at the end of the recorded run. */
+pbf_status pbf_backward(pbf_sim* sim, const float* dL_dx4, const float* dL_dv4, int where,
+                        float* dL_dx0_4, float* dL_dv0_4, pbf_param_grads* grads);
+
+/* Frees the recording of pbf_forward_record. */
+pbf_status pbf_release_record(pbf_sim* sim);
+
 /* ---- diagnostics ------------------------------------------------------------- */
 
 typedef struct pbf_diagnostics {

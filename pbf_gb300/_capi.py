@@ -71,6 +71,17 @@ class Tuning(C.Structure):
     ]
 
 
+class ParamGrads(C.Structure):
+    """pbf_param_grads (include/pbf.h)."""
+
+    _fields_ = [
+        ("epsilon", C.c_double),
+        ("tensile_instability_k", C.c_double),
+        ("xsph_viscosity_c", C.c_double),
+        ("vorticity_epsilon", C.c_double),
+    ]
+
+
 class Diagnostics(C.Structure):
     _fields_ = [
         ("mean_density_error", C.c_double),
@@ -122,6 +133,9 @@ SIGNATURES = {
     "pbf_radix_sort_noalloc": (C.c_int, [_P, _P, _P, C.c_uint32, C.c_uint32, _P]),
     "pbf_find_cells": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, _P]),
     "pbf_compute_diagnostics": (C.c_int, [_P, C.POINTER(Diagnostics)]),
+    "pbf_forward_record": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
+    "pbf_backward": (C.c_int, [_P, _P, _P, C.c_int, _P, _P, _P]),
+    "pbf_release_record": (C.c_int, [_P]),
     "pbf_status_string": (C.c_char_p, [C.c_int]),
     "pbf_last_error": (C.c_char_p, [_P]),
     "pbf_abi_version": (C.c_int, []),

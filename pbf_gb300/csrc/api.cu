@@ -14,6 +14,7 @@
 #include "../../include/pbf.h"
 #include "common.cuh"
 #include "internal.h"
+#include "sim.h"
 #include "sort.cuh"
 #include "substep.cuh"
 
@@ -27,59 +28,7 @@ thread_local std::string g_error;  // last error of calls without a handle
 
 void pbf::set_last_error(const char* msg) { g_error = msg ? msg : ""; }
 
-struct pbf_sim {
-    int device = 0;
-    cudaStream_t own_stream = nullptr;
-    cudaStream_t stream = nullptr;
-    pbf_params params{};  // scene 0; its iteration count and vorticity flag hold for all scenes
-    DevConsts dc{};       // scene 0's constants (the kernel parameter of a single scene)
-    uint32_t n = 0;
-    uint32_t ncells = 0;  // all scenes
-    uint32_t numbits = 0;
-    // several scenes in one handle (pbf_create_batch): concatenated scene-major
-    uint32_t nscenes = 1;
-    std::vector<pbf_params> sparams;
-    std::vector<DevConsts> sdc;
-    std::vector<uint32_t> counts, offsets;
-    DevConsts* d_consts = nullptr;  // [nscenes]
-    uint32_t* sid = nullptr;        // scene of each particle, id order
-    uint32_t* sid_sorted = nullptr; // scene of each particle, sorted order
-
-    // id-order state and predicted positions
-    float4 *x = nullptr, *v = nullptr, *xstar = nullptr;
-    // sorted-order buffers
-    float4 *XP = nullptr, *Pa = nullptr, *Pb = nullptr, *L = nullptr;
-    float4 *VS = nullptr, *VX = nullptr, *OM = nullptr, *Q = nullptr;
-    uint32_t *keys = nullptr, *skeys = nullptr, *perm = nullptr;
-    int32_t *cstart = nullptr, *cend = nullptr;
-    uint32_t* status = nullptr;  // device status word [0], bad-key flag [1]
-    // neighbour lists (pbf_tuning)
-    pbf_tuning tuning{};
-    uint32_t* nbr_idx = nullptr;
-    int32_t* nbr_cnt = nullptr;
-    uint32_t* guard = nullptr;
-    uint32_t nbr_cap = 0;       // capacity of nbr_idx in entries per particle
-    uint32_t guard_slots = 0;
-    uint32_t* h_status = nullptr;
-    void* sort_mem = nullptr;
-    SortWorkspace sort;
-
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    bool graph_valid = false;
-
-    bool timing = false;
-    std::vector<cudaEvent_t> ev;  // 7 + 2 * iterations stage boundaries
-    float ms[5] = {};             // reference phases of the last timed substep
-    double stage_ms[8] = {};      // stage sums since timing was enabled
-    uint32_t timed_substeps = 0;
-
-    std::string err;
-};
-
-namespace {
-
-pbf_status fail(pbf_sim* s, pbf_status st, const std::string& msg) {
+pbf_status pbf::fail(pbf_sim* s, pbf_status st, const std::string& msg) {
     if (s)
         s->err = msg;
     else
@@ -87,16 +36,15 @@ pbf_status fail(pbf_sim* s, pbf_status st, const std::string& msg) {
     return st;
 }
 
-pbf_status cuda_fail(pbf_sim* s, cudaError_t e, const char* what) {
+pbf_status pbf::cuda_fail(pbf_sim* s, cudaError_t e, const char* what) {
     std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
     return fail(s, e == cudaErrorMemoryAllocation ? PBF_ERR_OUT_OF_MEMORY : PBF_ERR_CUDA, msg);
 }
 
-#define PBF_CUDA(s, call)                                   \
-    do {                                                    \
-        cudaError_t e_ = (call);                            \
-        if (e_ != cudaSuccess) return cuda_fail((s), e_, #call); \
-    } while (0)
+
+
+namespace {
+
 
 pbf_status validate_params(const pbf_params* p, std::string& why) {
     if (!p) {
@@ -237,6 +185,7 @@ void free_sim(pbf_sim* s) {
     cudaGetDevice(&prev);
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
+    free_tape(s);
     if (s->exec) cudaGraphExecDestroy(s->exec);
     if (s->graph) cudaGraphDestroy(s->graph);
     void* bufs[] = {s->x,  s->v,  s->xstar, s->XP,   s->Pa,     s->Pb,   s->L,
@@ -254,17 +203,6 @@ void free_sim(pbf_sim* s) {
     delete s;
 }
 
-struct DeviceGuard {
-    int prev = -1;
-    explicit DeviceGuard(int dev) {
-        cudaGetDevice(&prev);
-        if (prev != dev) cudaSetDevice(dev);
-        else prev = -1;
-    }
-    ~DeviceGuard() {
-        if (prev >= 0) cudaSetDevice(prev);
-    }
-};
 
 // Kernel launches per substep (the sort's launches plus one per stage).
 uint32_t kernels_per_substep(const pbf_sim* s) {
@@ -274,102 +212,9 @@ uint32_t kernels_per_substep(const pbf_sim* s) {
            (s->params.vorticity_confinement ? 2u : 0u);
 }
 
-// Enqueues one substep (SPH::Run, src/SPH.cpp:246-334) on s->stream.  With
-// `ev` non-null, records an event at every stage boundary: before predict,
-// after predict, sort, cells, each lambda and delta-p launch, commit and the
-// two vorticity passes (7 + 2 * iterations events).
-template <class CPi, class CPs>
-cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const CPi& cpi, const CPs& cps) {
-    const uint32_t n = s->n;
-    if (!s->nbr_cnt || s->guard_slots < 2 + s->params.num_solver_iterations)
-        return cudaErrorInvalidValue;  // ensure_lists() runs before any capture
-    const unsigned g = grid_for(n);
-    const uint32_t iters = s->params.num_solver_iterations;
-    cudaStream_t st = s->stream;
-    auto mark = [&](uint32_t idx) {
-        if (ev) cudaEventRecord(ev[idx], st);
-    };
-    mark(0);
-    // 1 predict (predictpos.glsl)
-    launch_predict(g, st, s->x, s->v, s->xstar, s->keys, n, cpi, s->status);
-    mark(1);
-    // 2 sort (RadixSort::Run); first clear the cell starts of the previous
-    // substep while its sorted keys are still there
-    k_unmark_cells<<<g, kBlock, 0, st>>>(s->skeys, n, s->ncells, s->cstart);
-    cudaError_t e = sort_pairs(s->sort, s->keys, s->skeys, s->perm, n, s->numbits, s->status, st);
-    if (e != cudaSuccess) return e;
-    mark(2);
-    // 3 cell ranges (NeighbourCellFinder::FindNeighbourCells)
-    k_find_cells<<<g, kBlock, 0, st>>>(s->skeys, s->perm, s->xstar, s->XP, n, s->ncells, s->cstart,
-                                       s->cend, s->status + 1, s->sid, s->sid_sorted);
-    mark(3);
-    // 4 solver iterations (calclambda / updatepos).  The first lambda sweep
-    // also records the neighbour lists the later sweeps replay.
-    const NbrLists nl{s->nbr_idx, s->nbr_cnt, s->guard, s->nbr_cap, n};
-    cudaError_t ge = cudaMemsetAsync(s->guard, 0, sizeof(uint32_t) * (2 + iters), st);
-    if (ge != cudaSuccess) return ge;
-    const float4* cur = s->XP;
-    for (uint32_t it = 0; it < iters; ++it) {
-        float4* nxt = (it % 2 == 0) ? s->Pa : s->Pb;
-        const int in_slot = it == 0 ? -1 : (int)it;  // displacement of `cur` from XP
-        if (it == 0)
-            launch_lambda_build(g, st, s->XP, s->skeys, s->cstart, s->cend, s->L, nl, n, cps);
-        else
-            launch_lambda(g, st, cur, s->XP, s->skeys, s->cstart, s->cend, s->L, nl,
-                                           in_slot, n, cps);
-        mark(4 + 2 * it);
-        launch_delta_p(g, st, s->L, s->XP, s->skeys, s->cstart, s->cend, nxt, nl, in_slot,
-                                        (int)it + 1, n, cps, s->status);
-        mark(5 + 2 * it);
-        cur = nxt;
-    }
-    // 5 commit (update.glsl) and XSPH + vorticity (vorticity.glsl)
-    const bool vort = s->params.vorticity_confinement != 0;
-    const int fin_slot = iters == 0 ? -2 : (int)iters;  // -2: no list was built this substep
-    launch_commit(g, st, cur, s->perm, s->x, s->VS, vort ? nullptr : s->v, n, cps);
-    mark(4 + 2 * iters);
-    if (vort)
-        launch_vorticity_a(g, st, cur, s->XP, s->VS, s->skeys, s->cstart, s->cend, s->VX,
-                                            s->OM, s->Q, nl, fin_slot, n, cps);
-    mark(5 + 2 * iters);
-    if (vort)
-        launch_vorticity_b(g, st, s->Q, s->XP, s->VX, s->OM, s->skeys, s->perm, s->cstart,
-                                            s->cend, s->v, nl, fin_slot, n, cps);
-    mark(6 + 2 * iters);
-    return cudaGetLastError();
-}
-
-cudaError_t enqueue_substep(pbf_sim* s, cudaEvent_t* ev) {
-    if (s->nscenes == 1) return enqueue_impl(s, ev, OneScene{s->dc}, OneScene{s->dc});
-    return enqueue_impl(s, ev, ManyScenes{s->d_consts, s->sid},
-                        ManyScenes{s->d_consts, s->sid_sorted});
-}
-
 // One eager substep with stage events; accumulates the stage sums.
 pbf_status timed_substep(pbf_sim* s);
 
-void invalidate_graph(pbf_sim* s) {
-    if (s->exec) cudaGraphExecDestroy(s->exec);
-    if (s->graph) cudaGraphDestroy(s->graph);
-    s->exec = nullptr;
-    s->graph = nullptr;
-    s->graph_valid = false;
-}
-
-pbf_status check_status(pbf_sim* s) {
-    PBF_CUDA(s, cudaMemcpyAsync(s->h_status, s->status, 2 * sizeof(uint32_t),
-                                cudaMemcpyDeviceToHost, s->stream));
-    PBF_CUDA(s, cudaStreamSynchronize(s->stream));
-    const uint32_t bits = s->h_status[0];
-    if (bits & (kDevNonFinite | kDevSortTimeout)) {
-        std::string m = "device status";
-        if (bits & kDevNonFinite) m += ": non-finite position";
-        if (bits & kDevSortTimeout) m += ": radix-sort lookback timed out";
-        return fail(s, PBF_ERR_DEVICE_FAULT, m);
-    }
-    if (s->h_status[1]) return fail(s, PBF_ERR_DEVICE_FAULT, "device status: cell key out of range");
-    return PBF_OK;
-}
 
 pbf_status timed_substep(pbf_sim* s) {
     const uint32_t iters = s->params.num_solver_iterations;
@@ -406,6 +251,117 @@ pbf_status timed_substep(pbf_sim* s) {
 }
 
 }  // namespace
+
+namespace pbf {
+
+// Enqueues one substep (SPH::Run, src/SPH.cpp:246-334) on s->stream.  With
+// `ev` non-null, records an event at every stage boundary: before predict,
+// after predict, sort, cells, each lambda and delta-p launch, commit and the
+// two vorticity passes (7 + 2 * iterations events).
+template <class CPi, class CPs>
+cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, const CPi& cpi,
+                         const CPs& cps) {
+    const uint32_t n = s->n;
+    if (!s->nbr_cnt || s->guard_slots < 2 + s->params.num_solver_iterations)
+        return cudaErrorInvalidValue;  // ensure_lists() runs before any capture
+    const unsigned g = grid_for(n);
+    const uint32_t iters = s->params.num_solver_iterations;
+    cudaStream_t st = s->stream;
+    auto mark = [&](uint32_t idx) {
+        if (ev) cudaEventRecord(ev[idx], st);
+    };
+    mark(0);
+    // 1 predict (predictpos.glsl)
+    launch_predict(g, st, s->x, s->v, s->xstar, s->keys, n, cpi, s->status);
+    mark(1);
+    // 2 sort (RadixSort::Run); first clear the cell starts of the previous
+    // substep while its sorted keys are still there
+    k_unmark_cells<<<g, kBlock, 0, st>>>(s->skeys, n, s->ncells, s->cstart);
+    cudaError_t e = sort_pairs(s->sort, s->keys, s->skeys, s->perm, n, s->numbits, s->status, st);
+    if (e != cudaSuccess) return e;
+    mark(2);
+    // 3 cell ranges (NeighbourCellFinder::FindNeighbourCells)
+    k_find_cells<<<g, kBlock, 0, st>>>(s->skeys, s->perm, s->xstar, s->XP, n, s->ncells, s->cstart,
+                                       s->cend, s->status + 1, s->sid, s->sid_sorted);
+    mark(3);
+    // 4 solver iterations (calclambda / updatepos).  The first lambda sweep
+    // also records the neighbour lists the later sweeps replay.
+    const NbrLists nl{s->nbr_idx, s->nbr_cnt, s->guard, s->nbr_cap, n};
+    cudaError_t ge = cudaMemsetAsync(s->guard, 0, sizeof(uint32_t) * (2 + iters), st);
+    if (ge != cudaSuccess) return ge;
+    const float4* cur = s->XP;
+    for (uint32_t it = 0; it < iters; ++it) {
+        float4* nxt = (it % 2 == 0) ? s->Pa : s->Pb;
+        if (rec && it + 1 == iters) nxt = rec->PF;
+        float4* Lk = rec ? rec->L[it] : s->L;
+        float4* aux = rec ? rec->AUX[it] : nullptr;
+        const int in_slot = it == 0 ? -1 : (int)it;  // displacement of `cur` from XP
+        if (it == 0)
+            launch_lambda_build(g, st, s->XP, s->skeys, s->cstart, s->cend, Lk, aux, nl, n, cps);
+        else
+            launch_lambda(g, st, cur, s->XP, s->skeys, s->cstart, s->cend, Lk, aux, nl, in_slot, n,
+                          cps);
+        mark(4 + 2 * it);
+        launch_delta_p(g, st, Lk, s->XP, s->skeys, s->cstart, s->cend, nxt, nl, in_slot,
+                       (int)it + 1, n, cps, s->status);
+        mark(5 + 2 * it);
+        cur = nxt;
+    }
+    if (rec && iters == 0) {
+        cudaError_t ce = cudaMemcpyAsync(rec->PF, s->XP, sizeof(float4) * n,
+                                         cudaMemcpyDeviceToDevice, st);
+        if (ce != cudaSuccess) return ce;
+        cur = rec->PF;
+    }
+    // 5 commit (update.glsl) and XSPH + vorticity (vorticity.glsl)
+    const bool vort = s->params.vorticity_confinement != 0;
+    const int fin_slot = iters == 0 ? -2 : (int)iters;  // -2: no list was built this substep
+    float4* VS = rec ? rec->VS : s->VS;
+    float4* OM = rec ? rec->OM : s->OM;
+    float4* Q = rec ? rec->Q : s->Q;
+    launch_commit(g, st, cur, s->perm, s->x, VS, vort ? nullptr : s->v, n, cps);
+    mark(4 + 2 * iters);
+    if (vort)
+        launch_vorticity_a(g, st, cur, s->XP, VS, s->skeys, s->cstart, s->cend, s->VX, OM, Q, nl,
+                           fin_slot, n, cps);
+    mark(5 + 2 * iters);
+    if (vort)
+        launch_vorticity_b(g, st, Q, s->XP, s->VX, OM, s->skeys, s->perm, s->cstart, s->cend, s->v,
+                           rec ? rec->ETA : nullptr, nl, fin_slot, n, cps);
+    mark(6 + 2 * iters);
+    return cudaGetLastError();
+}
+
+cudaError_t enqueue_substep(pbf_sim* s, cudaEvent_t* ev, const Recording* rec) {
+    if (s->nscenes == 1) return enqueue_impl(s, ev, rec, OneScene{s->dc}, OneScene{s->dc});
+    return enqueue_impl(s, ev, rec, ManyScenes{s->d_consts, s->sid},
+                        ManyScenes{s->d_consts, s->sid_sorted});
+}
+
+void invalidate_graph(pbf_sim* s) {
+    if (s->exec) cudaGraphExecDestroy(s->exec);
+    if (s->graph) cudaGraphDestroy(s->graph);
+    s->exec = nullptr;
+    s->graph = nullptr;
+    s->graph_valid = false;
+}
+
+pbf_status check_status(pbf_sim* s) {
+    PBF_CUDA(s, cudaMemcpyAsync(s->h_status, s->status, 2 * sizeof(uint32_t),
+                                cudaMemcpyDeviceToHost, s->stream));
+    PBF_CUDA(s, cudaStreamSynchronize(s->stream));
+    const uint32_t bits = s->h_status[0];
+    if (bits & (kDevNonFinite | kDevSortTimeout)) {
+        std::string m = "device status";
+        if (bits & kDevNonFinite) m += ": non-finite position";
+        if (bits & kDevSortTimeout) m += ": radix-sort lookback timed out";
+        return fail(s, PBF_ERR_DEVICE_FAULT, m);
+    }
+    if (s->h_status[1]) return fail(s, PBF_ERR_DEVICE_FAULT, "device status: cell key out of range");
+    return PBF_OK;
+}
+
+}  // namespace pbf
 
 extern "C" {
 
@@ -549,6 +505,7 @@ pbf_status pbf_set_scene_params(pbf_sim* s, uint32_t scene, const pbf_params* p)
         PBF_CUDA(s, cudaMemcpy(s->d_consts + scene, &s->sdc[scene], sizeof(DevConsts),
                                cudaMemcpyHostToDevice));
     invalidate_graph(s);
+    free_tape(s);  // a recorded run is only valid for the parameters it ran with
     PBF_CUDA(s, ensure_lists(s));
     return PBF_OK;
 }

@@ -1,0 +1,59 @@
+// neighbours.cuh — the reference's neighbour enumeration, shared by the
+// forward stage kernels (substep.cu) and the adjoint kernels (adjoint.cu).
+#pragma once
+
+#include "common.cuh"
+
+namespace pbf {
+
+// Sorted-index ranges of the 9 stencil rows of a cell (neighbourcells.glsl:52-90).
+struct Runs {
+    int32_t b[9], e[9];
+};
+
+__device__ __forceinline__ void runs_of(uint32_t key, const DevConsts& c,
+                                        const int32_t* __restrict__ cstart,
+                                        const int32_t* __restrict__ cend, Runs& r) {
+    const uint32_t Gx = c.Gi[0], Gy = c.Gi[1], Gz = c.Gi[2];
+    const uint32_t local = key - c.cell_base;
+    const int cx = (int)(local % Gx);
+    const uint32_t rem = local / Gx;
+    const int cz = (int)(rem % Gz);
+    const int cy = (int)(rem / Gz);
+    const int xlo = cx > 0 ? cx - 1 : 0;
+    const int xhi = cx + 1 < (int)Gx ? cx + 1 : (int)Gx - 1;
+#pragma unroll
+    for (int o = 0; o < 9; ++o) {
+        const int ny = cy + (o / 3) - 1, nz = cz + (o % 3) - 1;
+        int32_t first = -1, last = -1;
+        if (ny >= 0 && ny < (int)Gy && nz >= 0 && nz < (int)Gz) {
+            const uint32_t base = c.cell_base + (uint32_t)ny * c.GxGz + (uint32_t)nz * Gx;
+            for (int xx = xlo; xx <= xhi; ++xx) {
+                const int32_t s = __ldg(cstart + base + (uint32_t)xx);
+                if (s != -1) {
+                    if (first == -1) first = s;
+                    last = __ldg(cend + base + (uint32_t)xx);
+                }
+            }
+        }
+        r.b[o] = first == -1 ? 0 : first;
+        r.e[o] = first == -1 ? 0 : last;
+    }
+}
+
+
+template <class F>
+__device__ __forceinline__ void visit_full(uint32_t i, uint32_t key, const DevConsts& c,
+                                           const int32_t* __restrict__ cstart,
+                                           const int32_t* __restrict__ cend, F&& f) {
+    // The 9 ranges live in a small local array: computing each row inside the
+    // loop instead raises register use and lowers occupancy (measured slower).
+    Runs r;
+    runs_of(key, c, cstart, cend, r);
+#pragma unroll 1
+    for (int o = 0; o < 9; ++o)
+        for (int32_t j = r.b[o]; j < r.e[o]; ++j)
+            if ((uint32_t)j != i) f((uint32_t)j);
+}
+
+}  // namespace pbf

@@ -1,0 +1,117 @@
+// sim.h — the pbf_sim handle and the host helpers shared by api.cu and
+// adjoint.cu (internal; not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/pbf.h"
+#include "common.cuh"
+#include "sort.cuh"
+
+namespace pbf {
+struct Tape;  // adjoint.cu
+}
+
+using pbf::DevConsts;
+using pbf::SortWorkspace;
+
+struct pbf_sim {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    pbf_params params{};  // scene 0; its iteration count and vorticity flag hold for all scenes
+    DevConsts dc{};       // scene 0's constants (the kernel parameter of a single scene)
+    uint32_t n = 0;
+    uint32_t ncells = 0;  // all scenes
+    uint32_t numbits = 0;
+    // several scenes in one handle (pbf_create_batch): concatenated scene-major
+    uint32_t nscenes = 1;
+    std::vector<pbf_params> sparams;
+    std::vector<DevConsts> sdc;
+    std::vector<uint32_t> counts, offsets;
+    DevConsts* d_consts = nullptr;  // [nscenes]
+    uint32_t* sid = nullptr;        // scene of each particle, id order
+    uint32_t* sid_sorted = nullptr; // scene of each particle, sorted order
+
+    // id-order state and predicted positions
+    float4 *x = nullptr, *v = nullptr, *xstar = nullptr;
+    // sorted-order buffers
+    float4 *XP = nullptr, *Pa = nullptr, *Pb = nullptr, *L = nullptr;
+    float4 *VS = nullptr, *VX = nullptr, *OM = nullptr, *Q = nullptr;
+    uint32_t *keys = nullptr, *skeys = nullptr, *perm = nullptr;
+    int32_t *cstart = nullptr, *cend = nullptr;
+    uint32_t* status = nullptr;  // device status word [0], bad-key flag [1]
+    // neighbour lists (pbf_tuning)
+    pbf_tuning tuning{};
+    uint32_t* nbr_idx = nullptr;
+    int32_t* nbr_cnt = nullptr;
+    uint32_t* guard = nullptr;
+    uint32_t nbr_cap = 0;       // capacity of nbr_idx in entries per particle
+    uint32_t guard_slots = 0;
+    uint32_t* h_status = nullptr;
+    void* sort_mem = nullptr;
+    SortWorkspace sort;
+
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool graph_valid = false;
+
+    bool timing = false;
+    std::vector<cudaEvent_t> ev;  // 7 + 2 * iterations stage boundaries
+    float ms[5] = {};             // reference phases of the last timed substep
+    double stage_ms[8] = {};      // stage sums since timing was enabled
+    uint32_t timed_substeps = 0;
+
+    pbf::Tape* tape = nullptr;  // recorded forward run for pbf_backward
+
+    std::string err;
+};
+
+namespace pbf {
+
+// Where a recorded substep stores what the adjoint needs (sorted order):
+// L[k] = (x, y, z, lambda) and AUX[k] = (sum_j grad C_i, sum |grad C|^2 + |sum grad C|^2)
+// of solver iteration k, the final positions, and the vorticity pass outputs.
+struct Recording {
+    float4* const* L = nullptr;    // [iterations]
+    float4* const* AUX = nullptr;  // [iterations]
+    float4* PF = nullptr;
+    float4* VS = nullptr;
+    float4* OM = nullptr;
+    float4* Q = nullptr;
+    float4* ETA = nullptr;
+};
+
+pbf_status fail(pbf_sim* s, pbf_status st, const std::string& msg);
+pbf_status cuda_fail(pbf_sim* s, cudaError_t e, const char* what);
+pbf_status check_status(pbf_sim* s);
+// Enqueues one substep on s->stream; with `rec`, the stage outputs land in
+// the recording's buffers.  `ev`: optional stage events (timing mode).
+cudaError_t enqueue_substep(pbf_sim* s, cudaEvent_t* ev, const Recording* rec = nullptr);
+void invalidate_graph(pbf_sim* s);
+void free_tape(pbf_sim* s);
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev)
+            cudaSetDevice(dev);
+        else
+            prev = -1;
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+}  // namespace pbf
+
+#define PBF_CUDA(s, call)                                                \
+    do {                                                                 \
+        cudaError_t e_ = (call);                                         \
+        if (e_ != cudaSuccess) return ::pbf::cuda_fail((s), e_, #call);  \
+    } while (0)

@@ -17,45 +17,11 @@
 // each row's up-to-3-cell x-run in ascending sorted index, skipping i itself
 // (foreachneighbour.glsl:1-10), and accumulates in that order.
 #include "substep.cuh"
+#include "neighbours.cuh"
 
 namespace pbf {
 
 namespace {
-
-// Sorted-index ranges of the 9 stencil rows of a cell (neighbourcells.glsl:52-90).
-struct Runs {
-    int32_t b[9], e[9];
-};
-
-__device__ __forceinline__ void runs_of(uint32_t key, const DevConsts& c,
-                                        const int32_t* __restrict__ cstart,
-                                        const int32_t* __restrict__ cend, Runs& r) {
-    const uint32_t Gx = c.Gi[0], Gy = c.Gi[1], Gz = c.Gi[2];
-    const uint32_t local = key - c.cell_base;
-    const int cx = (int)(local % Gx);
-    const uint32_t rem = local / Gx;
-    const int cz = (int)(rem % Gz);
-    const int cy = (int)(rem / Gz);
-    const int xlo = cx > 0 ? cx - 1 : 0;
-    const int xhi = cx + 1 < (int)Gx ? cx + 1 : (int)Gx - 1;
-#pragma unroll
-    for (int o = 0; o < 9; ++o) {
-        const int ny = cy + (o / 3) - 1, nz = cz + (o % 3) - 1;
-        int32_t first = -1, last = -1;
-        if (ny >= 0 && ny < (int)Gy && nz >= 0 && nz < (int)Gz) {
-            const uint32_t base = c.cell_base + (uint32_t)ny * c.GxGz + (uint32_t)nz * Gx;
-            for (int xx = xlo; xx <= xhi; ++xx) {
-                const int32_t s = __ldg(cstart + base + (uint32_t)xx);
-                if (s != -1) {
-                    if (first == -1) first = s;
-                    last = __ldg(cend + base + (uint32_t)xx);
-                }
-            }
-        }
-        r.b[o] = first == -1 ? 0 : first;
-        r.e[o] = first == -1 ? 0 : last;
-    }
-}
 
 }  // namespace
 
@@ -138,20 +104,6 @@ k_find_cells(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ pe
 // visitors therefore produce the same sums, bit for bit.
 
 template <class F>
-__device__ __forceinline__ void visit_full(uint32_t i, uint32_t key, const DevConsts& c,
-                                           const int32_t* __restrict__ cstart,
-                                           const int32_t* __restrict__ cend, F&& f) {
-    // The 9 ranges live in a small local array: computing each row inside the
-    // loop instead raises register use and lowers occupancy (measured slower).
-    Runs r;
-    runs_of(key, c, cstart, cend, r);
-#pragma unroll 1
-    for (int o = 0; o < 9; ++o)
-        for (int32_t j = r.b[o]; j < r.e[o]; ++j)
-            if ((uint32_t)j != i) f((uint32_t)j);
-}
-
-template <class F>
 __device__ __forceinline__ void visit_list(uint32_t i, int32_t cnt, const NbrLists& nl, F&& f) {
     const uint32_t* __restrict__ p = nl.idx + i;
     for (int32_t k = 0; k < cnt; ++k) f(__ldg(p + (size_t)k * nl.n));
@@ -196,6 +148,13 @@ __device__ __forceinline__ void lambda_pair(const DevConsts& c, float3 d, float 
     a.gi = add3(a.gi, g);                  // :93
 }
 
+// What the adjoint needs of a lambda evaluation: sum_j grad_pj C_i (the
+// gradient w.r.t. p_i, calclambda.glsl:93) and the full denominator sum
+// before epsilon (:89,97).
+__device__ __forceinline__ float4 lambda_aux(const LambdaAcc& a) {
+    return make_float4(a.gi.x, a.gi.y, a.gi.z, fadd(a.sumk, dot3(a.gi, a.gi)));
+}
+
 // calclambda.glsl:97-101
 __device__ __forceinline__ float lambda_finish(const DevConsts& c, const LambdaAcc& a) {
     const float sumk = fadd(a.sumk, dot3(a.gi, a.gi));  // :97
@@ -222,7 +181,7 @@ template <class CP>
 __global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
 k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys,
                const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
-               float4* __restrict__ L, NbrLists nl, uint32_t n, CP cp) {
+               float4* __restrict__ L, float4* __restrict__ aux, NbrLists nl, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < n;
     float3 pi = make_float3(0.0f, 0.0f, 0.0f);
@@ -243,6 +202,7 @@ k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys
         });
         nl.cnt[i] = (uint32_t)cnt <= cap ? cnt : -1;
         L[i] = make_float4(pi.x, pi.y, pi.z, lambda_finish(c, a));
+        if (aux) aux[i] = lambda_aux(a);
     }
     const float m = fmaxf(fmaxf(fabsf(pi.x), fabsf(pi.y)), fabsf(pi.z));
     warp_max_to(nl.guard, m);
@@ -254,8 +214,8 @@ template <class CP>
 __global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
 k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
          const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cstart,
-         const int32_t* __restrict__ cend, float4* __restrict__ L, NbrLists nl, int dmax_slot,
-         uint32_t n, CP cp) {
+         const int32_t* __restrict__ cend, float4* __restrict__ L, float4* __restrict__ aux,
+         NbrLists nl, int dmax_slot, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const auto& c = cp.at(i);
@@ -271,6 +231,7 @@ k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
     else
         visit_full(i, skeys[i], c, cstart, cend, body);
     L[i] = make_float4(pi.x, pi.y, pi.z, lambda_finish(c, a));
+    if (aux) aux[i] = lambda_aux(a);
 }
 
 // updatepos.glsl:42-104.  Reads L = (p, lambda), writes clamped positions Pn
@@ -394,7 +355,8 @@ k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ XP,
               const float4* __restrict__ VX, const float4* __restrict__ OM,
               const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
-              float4* __restrict__ v, NbrLists nl, int dmax_slot, uint32_t n, CP cp) {
+              float4* __restrict__ v, float4* __restrict__ eta_out, NbrLists nl, int dmax_slot,
+              uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const auto& c = cp.at(i);
@@ -415,6 +377,7 @@ k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ XP,
         visit_list(i, cnt, nl, body);
     else
         visit_full(i, skeys[i], c, cstart, cend, body);
+    if (eta_out) eta_out[i] = make_float4(eta.x, eta.y, eta.z, 0.0f);
     const float l = fsqrt(dot3(eta, eta));  // :76
     if (l > 0.0f) eta = make_float3(fdiv(eta.x, l), fdiv(eta.y, l), fdiv(eta.z, l));  // :77-78
     const float3 vf = fma3(c.dteps, cross3(eta, xyz(OM[i])), xyz(VX[i]));  // :82
@@ -466,15 +429,15 @@ void launch_keys_of(unsigned g, cudaStream_t st, const float4* x, float4* xstar,
 }
 template <class CP>
 void launch_lambda_build(unsigned g, cudaStream_t st, const float4* XP, const uint32_t* skeys,
-                         const int32_t* cstart, const int32_t* cend, float4* L, NbrLists nl,
-                         uint32_t n, CP cp) {
-    k_lambda_build<CP><<<g, kBlock, 0, st>>>(XP, skeys, cstart, cend, L, nl, n, cp);
+                         const int32_t* cstart, const int32_t* cend, float4* L, float4* aux,
+                         NbrLists nl, uint32_t n, CP cp) {
+    k_lambda_build<CP><<<g, kBlock, 0, st>>>(XP, skeys, cstart, cend, L, aux, nl, n, cp);
 }
 template <class CP>
 void launch_lambda(unsigned g, cudaStream_t st, const float4* P, const float4* XP,
                    const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* L,
-                   NbrLists nl, int dmax_slot, uint32_t n, CP cp) {
-    k_lambda<CP><<<g, kBlock, 0, st>>>(P, XP, skeys, cstart, cend, L, nl, dmax_slot, n, cp);
+                   float4* aux, NbrLists nl, int dmax_slot, uint32_t n, CP cp) {
+    k_lambda<CP><<<g, kBlock, 0, st>>>(P, XP, skeys, cstart, cend, L, aux, nl, dmax_slot, n, cp);
 }
 template <class CP>
 void launch_delta_p(unsigned g, cudaStream_t st, const float4* L, const float4* XP,
@@ -500,9 +463,10 @@ template <class CP>
 void launch_vorticity_b(unsigned g, cudaStream_t st, const float4* Q, const float4* XP,
                         const float4* VX, const float4* OM, const uint32_t* skeys,
                         const uint32_t* perm, const int32_t* cstart, const int32_t* cend,
-                        float4* v, NbrLists nl, int dmax_slot, uint32_t n, CP cp) {
-    k_vorticity_b<CP><<<g, kBlock, 0, st>>>(Q, XP, VX, OM, skeys, perm, cstart, cend, v, nl,
-                                            dmax_slot, n, cp);
+                        float4* v, float4* eta_out, NbrLists nl, int dmax_slot, uint32_t n,
+                        CP cp) {
+    k_vorticity_b<CP><<<g, kBlock, 0, st>>>(Q, XP, VX, OM, skeys, perm, cstart, cend, v, eta_out,
+                                            nl, dmax_slot, n, cp);
 }
 template <class CP>
 void launch_diagnostics(unsigned g, cudaStream_t st, const float4* P, const float4* v,
@@ -517,11 +481,11 @@ void launch_diagnostics(unsigned g, cudaStream_t st, const float4* P, const floa
     template void launch_keys_of<CP>(unsigned, cudaStream_t, const float4*, float4*, uint32_t*, \
                                      uint32_t, CP);                                             \
     template void launch_lambda_build<CP>(unsigned, cudaStream_t, const float4*, const uint32_t*, \
-                                          const int32_t*, const int32_t*, float4*, NbrLists,    \
-                                          uint32_t, CP);                                        \
+                                          const int32_t*, const int32_t*, float4*, float4*,     \
+                                          NbrLists, uint32_t, CP);                              \
     template void launch_lambda<CP>(unsigned, cudaStream_t, const float4*, const float4*,       \
                                     const uint32_t*, const int32_t*, const int32_t*, float4*,   \
-                                    NbrLists, int, uint32_t, CP);                               \
+                                    float4*, NbrLists, int, uint32_t, CP);                      \
     template void launch_delta_p<CP>(unsigned, cudaStream_t, const float4*, const float4*,      \
                                      const uint32_t*, const int32_t*, const int32_t*, float4*,  \
                                      NbrLists, int, int, uint32_t, CP, uint32_t*);              \
@@ -534,7 +498,7 @@ void launch_diagnostics(unsigned g, cudaStream_t st, const float4* P, const floa
     template void launch_vorticity_b<CP>(unsigned, cudaStream_t, const float4*, const float4*,  \
                                          const float4*, const float4*, const uint32_t*,         \
                                          const uint32_t*, const int32_t*, const int32_t*,       \
-                                         float4*, NbrLists, int, uint32_t, CP);                 \
+                                         float4*, float4*, NbrLists, int, uint32_t, CP);        \
     template void launch_diagnostics<CP>(unsigned, cudaStream_t, const float4*, const float4*,  \
                                          const uint32_t*, const uint32_t*, const int32_t*,      \
                                          const int32_t*, float4*, uint32_t, CP);

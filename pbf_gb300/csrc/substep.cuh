@@ -24,12 +24,12 @@ void launch_keys_of(unsigned g, cudaStream_t st, const float4* x, float4* xstar,
                     uint32_t n, CP cp);
 template <class CP>
 void launch_lambda_build(unsigned g, cudaStream_t st, const float4* XP, const uint32_t* skeys,
-                         const int32_t* cstart, const int32_t* cend, float4* L, NbrLists nl,
-                         uint32_t n, CP cp);
+                         const int32_t* cstart, const int32_t* cend, float4* L, float4* aux,
+                         NbrLists nl, uint32_t n, CP cp);
 template <class CP>
 void launch_lambda(unsigned g, cudaStream_t st, const float4* P, const float4* XP,
                    const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* L,
-                   NbrLists nl, int dmax_slot, uint32_t n, CP cp);
+                   float4* aux, NbrLists nl, int dmax_slot, uint32_t n, CP cp);
 template <class CP>
 void launch_delta_p(unsigned g, cudaStream_t st, const float4* L, const float4* XP,
                     const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* Pn,
@@ -46,7 +46,8 @@ template <class CP>
 void launch_vorticity_b(unsigned g, cudaStream_t st, const float4* Q, const float4* XP,
                         const float4* VX, const float4* OM, const uint32_t* skeys,
                         const uint32_t* perm, const int32_t* cstart, const int32_t* cend,
-                        float4* v, NbrLists nl, int dmax_slot, uint32_t n, CP cp);
+                        float4* v, float4* eta_out, NbrLists nl, int dmax_slot, uint32_t n,
+                        CP cp);
 template <class CP>
 void launch_diagnostics(unsigned g, cudaStream_t st, const float4* P, const float4* v,
                         const uint32_t* skeys, const uint32_t* perm, const int32_t* cstart,

@@ -18,7 +18,8 @@ import ctypes as C
 
 import numpy as np
 
-from ._capi import (PBF_DEVICE, PBF_HOST, Diagnostics, Params, PbfError, Tuning, check, load)
+from ._capi import (PBF_DEVICE, PBF_HOST, Diagnostics, ParamGrads, Params, PbfError, Tuning,
+                    check, load)
 
 
 def default_params(gridsize=(128, 64, 128)) -> Params:
@@ -255,6 +256,41 @@ class SPH:
 
     def kernels_per_substep(self) -> int:
         return int(self._lib.pbf_kernels_per_substep(self._h))
+
+    # ---- differentiation ------------------------------------------------------
+    PARAM_NAMES = ("epsilon", "tensile_instability_k", "xsph_viscosity_c", "vorticity_epsilon")
+
+    def forward_record(self, substeps: int, checkpoint_every: int = 8) -> None:
+        """Steps like step() and records what backward() needs (pbf_forward_record)."""
+        check(self._lib.pbf_forward_record(self._h, int(substeps), int(checkpoint_every)),
+              self._h)
+
+    def backward(self, dL_dx=None, dL_dv=None):
+        """Gradients at the start of the recorded run: (dL/dx0, dL/dv0, per-scene
+        parameter gradients as an (num_scenes, 4) array in PARAM_NAMES order)."""
+        n = self._n
+        gx = None if dL_dx is None else _as_f4(dL_dx, n)
+        gv = None if dL_dv is None else _as_f4(dL_dv, n)
+        dx0 = np.empty((n, 4), np.float32)
+        dv0 = np.empty((n, 4), np.float32)
+        ns = int(self._lib.pbf_num_scenes(self._h))
+        grads = (ParamGrads * ns)()
+        check(self._lib.pbf_backward(self._h, None if gx is None else gx.ctypes.data,
+                                     None if gv is None else gv.ctypes.data, PBF_HOST,
+                                     dx0.ctypes.data, dv0.ctypes.data, grads), self._h)
+        g = np.array([[getattr(grads[k], nm) for nm in self.PARAM_NAMES] for k in range(ns)])
+        return dx0, dv0, g
+
+    def backward_device(self, gx_ptr, gv_ptr, dx0_ptr, dv0_ptr):
+        """backward() on device buffers (float4, id order); returns the parameter gradients."""
+        ns = int(self._lib.pbf_num_scenes(self._h))
+        grads = (ParamGrads * ns)()
+        check(self._lib.pbf_backward(self._h, gx_ptr, gv_ptr, PBF_DEVICE, dx0_ptr, dv0_ptr, grads),
+              self._h)
+        return np.array([[getattr(grads[k], nm) for nm in self.PARAM_NAMES] for k in range(ns)])
+
+    def release_record(self) -> None:
+        check(self._lib.pbf_release_record(self._h), self._h)
 
     # ---- debug reads of the last substep ---------------------------------------
     def get_sort(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
