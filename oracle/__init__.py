@@ -7,11 +7,11 @@ it, and only as the checker or the timed CPU baseline: the product
 (pbf_gb300/) never imports, links or calls it.
 
 Parity status: the reference runs only inside an OpenGL 4.3 context, which
-neither machine here has, and it ships no tests or golden vectors.  The
-oracle is pinned by known-answer tests derived from the shader source (kernel
-constants, the rest-lattice density, hand-built sort and cell-range cases)
-and by committed fixtures it generated (tests/golden/), not by outputs of the
-reference itself.
+neither machine here has, and it ships no tests or golden vectors.  Its
+compute shaders are compiled as C++ by ref_build.py (from the reference
+checkout, interface declarations rewritten, bodies as written) and the oracle
+is checked against them (tests/test_ref_pin.py); their outputs are committed
+as fixtures (tests/golden/).
 """
 from __future__ import annotations
 
@@ -180,3 +180,51 @@ def radix_sort(keys, numbits: int):
 
 def params_size() -> int:
     return int(load().pbfo_params_size())
+
+
+# ---- the reference's own shaders compiled as C++ (oracle/ref_build.py) ---------
+
+def ref_available() -> bool:
+    """True when the reference checkout is present here (the library is built
+    from its shader files; it cannot be built where the checkout is absent)."""
+    from . import ref_build
+    return ref_build.available()
+
+
+_ref = None
+
+
+def ref_load() -> C.CDLL:
+    global _ref
+    if _ref is None:
+        from . import ref_build
+        path = ref_build.build()
+        if path is None:
+            raise RuntimeError("the reference checkout is absent: its shaders cannot be built")
+        lib = C.CDLL(path)
+        P = C.c_void_p
+        lib.pbfr_substep.argtypes = [P, C.c_uint32, P, P, P, P, P, P, P]
+        lib.pbfr_substep.restype = C.c_int
+        _ref = lib
+    return _ref
+
+
+def ref_substep(params, x4, v4):
+    """One SPH::Run of the reference's shaders.  Returns a dict with x, v (id
+    order), sorted ids, the grid start/end textures (x fastest, then y, z),
+    the packed neighbour texture (n, 3, 4) and lambda (sorted order)."""
+    lib = ref_load()
+    n = x4.shape[0]
+    x = np.ascontiguousarray(x4, np.float32).copy()
+    v = np.ascontiguousarray(v4, np.float32).copy()
+    g = [int(a) for a in params.grid]
+    cells = g[0] * g[1] * g[2]
+    ids = np.empty(n, np.uint32)
+    st = np.empty(cells, np.int32)
+    en = np.empty(cells, np.int32)
+    nbr = np.empty(12 * n, np.int32)
+    lam = np.empty(n, np.float32)
+    lib.pbfr_substep(C.addressof(params), n, x.ctypes.data, v.ctypes.data, ids.ctypes.data,
+                     st.ctypes.data, en.ctypes.data, nbr.ctypes.data, lam.ctypes.data)
+    return {"x": x, "v": v, "ids": ids, "start": st.reshape(g[2], g[1], g[0]),
+            "end": en.reshape(g[2], g[1], g[0]), "nbr": nbr.reshape(n, 3, 4), "lambda": lam}

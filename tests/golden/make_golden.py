@@ -1,0 +1,40 @@
+"""Generates the golden fixtures: outputs of the reference's own compute
+shaders (compiled as C++ from the reference checkout by oracle/ref_build.py)
+for one substep of each scene in pin_scenes.py.  Run here, where the
+reference checkout exists; the fixtures then travel to machines that lack it.
+
+    python tests/golden/make_golden.py
+"""
+import hashlib
+import json
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+sys.path.insert(0, HERE)
+
+import numpy as np  # noqa: E402
+
+import oracle  # noqa: E402
+import pin_scenes  # noqa: E402
+
+
+def main():
+    manifest = {}
+    for name in pin_scenes.CASES:
+        p, x4, v4 = pin_scenes.make(name)
+        r = oracle.ref_substep(p, x4, v4)
+        path = os.path.join(HERE, f"ref_{name}.npz")
+        np.savez_compressed(path, x_in=x4, v_in=v4, x=r["x"], v=r["v"], ids=r["ids"],
+                            lam=r["lambda"])
+        manifest[os.path.basename(path)] = hashlib.sha256(open(path, "rb").read()).hexdigest()
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py",
+                   "source": "reference shaders compiled by oracle/ref_build.py",
+                   "sha256": manifest}, f, indent=1)
+    print(json.dumps(manifest, indent=1))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,96 @@
+"""The oracle against the reference's own compute shaders.
+
+oracle/ref_build.py compiles the reference's shader files, as written, into a
+CPU library (interface declarations rewritten, bodies untouched), and
+tests/golden/ holds that library's outputs for one substep of each scene in
+tests/golden/pin_scenes.py.  These tests pin the oracle -- and through the
+bit-exact GPU tests the CUDA kernels -- to the reference's code:
+- the sort order and the cell-start texture are identical;
+- the neighbour runs are identical (except the last-cell dummy, whose `end`
+  the reference never writes);
+- positions agree within the benchmark spec's tolerance 1e-5 h, lambda and
+  velocities within their rounding (the shaders round each operation in
+  source order; the oracle fuses the multiply-adds it lists).
+"""
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import oracle
+
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+sys.path.insert(0, HERE)
+import pin_scenes  # noqa: E402
+
+CASES = list(pin_scenes.CASES)
+
+
+def golden(name):
+    return np.load(os.path.join(HERE, f"ref_{name}.npz"))
+
+
+def test_golden_manifest():
+    m = json.load(open(os.path.join(HERE, "manifest.json")))
+    for fn, digest in m["sha256"].items():
+        assert hashlib.sha256(open(os.path.join(HERE, fn), "rb").read()).hexdigest() == digest, fn
+    assert set(m["sha256"]) == {f"ref_{c}.npz" for c in CASES}
+
+
+def tolerances(p):
+    h = float(p.h)
+    return {"x": 1e-5 * h, "v": 1e-5 * h / float(p.timestep), "lam": 2e-5}
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_matches_reference_golden(oracle_mod, name):
+    p, x4, v4 = pin_scenes.make(name)
+    g = golden(name)
+    assert np.array_equal(g["x_in"], x4) and np.array_equal(g["v_in"], v4)
+    o = oracle_mod.Oracle(p, x4.shape[0])
+    o.set_state(x4, v4)
+    o.step(1)
+    _, _, perm = o.get_sort()
+    assert np.array_equal(perm, g["ids"]), "sort order differs from the reference's"
+    x, v = o.get_state()
+    lam, _ = o.get_solver()
+    tol = tolerances(p)
+    assert np.max(np.abs(x[:, :3] - g["x"][:, :3])) <= tol["x"]
+    assert np.max(np.abs(v[:, :3] - g["v"][:, :3])) <= tol["v"]
+    if p.num_solver_iterations:
+        assert np.max(np.abs(lam - g["lam"])) <= tol["lam"]
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="the reference checkout is not on this machine")
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_matches_live_reference_shaders(oracle_mod, name):
+    p, x4, v4 = pin_scenes.make(name)
+    r = oracle_mod.ref_substep(p, x4, v4)
+    o = oracle_mod.Oracle(p, x4.shape[0])
+    o.set_state(x4, v4)
+    o.step(1)
+    st, en = o.get_cells()
+    G = [int(a) for a in p.grid]
+    zz, yy, xx = np.meshgrid(np.arange(G[2]), np.arange(G[1]), np.arange(G[0]), indexing="ij")
+    key = xx + zz * G[0] + yy * G[0] * G[2]
+    assert np.array_equal(r["start"], st[key]), "cell-start texture differs"
+    occupied = (st[key] >= 0)
+    occupied[-1, -1, -1] = False  # the reference never writes the last cell's end
+    assert np.array_equal(r["end"][occupied], en[key][occupied]), "cell-end texture differs"
+    n = x4.shape[0]
+    for i in range(n - 1):  # the last sorted particle is the last-cell dummy
+        runs = o.get_runs(i)
+        for row in range(9):
+            pk = int(r["nbr"][i, row // 3, row % 3])
+            rs, re_ = (0, 0) if pk == -1 else (pk & 0xFFFFFF, (pk & 0xFFFFFF) + (pk >> 24))
+            b, e = (int(v) for v in runs[row])
+            assert (rs, re_) == (b, e) or (b == e and rs == re_), (i, row, (rs, re_), (b, e))
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="the reference checkout is not on this machine")
+def test_reference_library_rebuilds_from_the_checkout():
+    from oracle import ref_build
+    assert ref_build.build() is not None
