@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--no-stable", action="store_true", help="skip the epsilon = 5 full run")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-scene comparison")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the backward/forward ratio")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--recovery", action="store_true",
                     help="also run the 64-scene parameter recovery (about a minute)")
     return ap.parse_args()
@@ -256,9 +257,11 @@ def adjoint_ratio(stream, substeps: int = 64, every: int = 8):
             "checkpoint_every": every, "forward_ms": f * 1e3, "backward_ms": bk * 1e3,
             "bwd_fwd_ratio": bk / f, "loss": loss,
             "grad_norm_v0": float(np.linalg.norm(dv0[:, :3])),
+            "grad_finite": bool(np.all(np.isfinite(dv0))),
             "grad_params": dict(zip(pg.SPH.PARAM_NAMES, [float(v) for v in g[0]])),
             "note": "wall-clock per call, host synchronised; backward includes the "
-                    "recomputation of every checkpoint segment"}
+                    "recomputation of every checkpoint segment; with epsilon = 0.01 the "
+                    "64-substep derivative overflows FP32 (the run blows up)"}
 
 
 def recovery(stream, num_scenes: int = 64, substeps: int = 32, steps: int = 50, seed: int = 11,
@@ -425,7 +428,11 @@ def main():
     sim = pg.SPH(scene.n, tuple(scene.params.grid), scene.params)
     sim.set_stream(stream.cuda_stream)
 
-    # warm-up (captures the graph), then reset to the initial scene
+    # warm-up: the autotuner picks block size and neighbour-list settings on
+    # the first substeps of this scene (no setting changes any result), then
+    # W substeps under the chosen tuning capture the graph; reset after
+    sim.set_state(scene.x4, scene.v4)
+    tuning = sim.autotune(10) if not args.no_autotune else None
     sim.set_state(scene.x4, scene.v4)
     sim.step(W)
     sim.synchronize()
@@ -506,6 +513,8 @@ def main():
         ps.epsilon = 5.0
         sim.set_params(ps)
         sim.set_state(scene.x4, scene.v4)
+        stable_tuning = sim.autotune(10) if not args.no_autotune else None
+        sim.set_state(scene.x4, scene.v4)
         sim.step(3)
         sim.set_state(scene.x4, scene.v4)
         torch.cuda.synchronize()
@@ -519,8 +528,9 @@ def main():
         sms = g0.elapsed_time(g1)
         stable = {"value": scene.n * it * scene.substeps / (sms * 1e-3), "unit": UNIT,
                   "substeps": scene.substeps, "ms_per_step": sms / scene.substeps,
-                  "epsilon": 5.0, "note": "same scene and constants except CFM epsilon = 5 "
-                                          "(src/SPH.cpp:138), full run"}
+                  "epsilon": 5.0, "tuning": stable_tuning,
+                  "note": "same scene and constants except CFM epsilon = 5 "
+                          "(src/SPH.cpp:138), full run"}
         sim.set_params(scene.params)
 
     adjoint = None
@@ -552,7 +562,8 @@ def main():
                        "grid": list(scene.params.grid), "dt": scene.params.timestep,
                        "substeps_timed": K, "window": f"substeps 1-{K} of {scene.substeps}",
                        "l2": "working set > L2 (no flush)",
-                       "parallelism": "replicas" if world > 1 else "single"},
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "tuning": tuning},
             "e2e": {"value": e2e_value, "unit": UNIT,
                     "h2d_bytes_per_step": 2 * 16 * scene.n, "d2h_bytes_per_step": 2 * 16 * scene.n,
                     "ms_per_step": e2e_ms / E, "steps": E},

@@ -189,11 +189,21 @@ typedef struct pbf_tuning {
     uint32_t list_capacity;       /* entries per particle; longer lists fall back to the
                                      full stencil scan for that particle */
     float skin_h;                 /* list radius is h * (1 + skin_h) */
+    uint32_t block_size;          /* threads per block of the neighbour sweeps: a
+                                     multiple of 32 in [32, 256]; 0 = 256 */
 } pbf_tuning;
 
 /* No reference counterpart (the reference has no tuning surface). */
 pbf_status pbf_set_tuning(pbf_sim* sim, const pbf_tuning* tuning);
 pbf_status pbf_get_tuning(const pbf_sim* sim, pbf_tuning* out);
+
+/* Autotuner: times `trial_substeps` substeps from the current state under
+ * each candidate tuning (sweep block size 128 / 256; neighbour lists off, or
+ * on with skin 0.05h / 0.1h / 0.2h), restoring the state before every trial
+ * and after the last, and keeps the fastest, which it also writes to `best`
+ * (may be NULL).  The state is unchanged on return.  Since no tuning changes
+ * any result, tuning never changes a simulation. */
+pbf_status pbf_autotune(pbf_sim* sim, uint32_t trial_substeps, pbf_tuning* best);
 
 /* Waits for the handle's stream and reports the device status word. */
 pbf_status pbf_synchronize(pbf_sim* sim);
@@ -319,6 +329,11 @@ pbf_status pbf_compute_diagnostics(pbf_sim* sim, pbf_diagnostics* out);
 /* ---- errors ------------------------------------------------------------------ */
 
 const char* pbf_status_string(pbf_status status);
+
+/* Host-side fault injection for tests (no reference counterpart): the
+ * `after`-th device allocation made by the library from now on (0 = the next
+ * one) fails as out of memory, without reaching the device; negative disarms. */
+void pbf_debug_fail_allocation(int after);
 /* Message of the last failed call on `sim`, or of the last failed call
  * without a handle when sim is NULL.  Never NULL. */
 const char* pbf_last_error(const pbf_sim* sim);

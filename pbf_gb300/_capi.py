@@ -68,6 +68,7 @@ class Tuning(C.Structure):
         ("use_neighbour_lists", C.c_uint32),
         ("list_capacity", C.c_uint32),
         ("skin_h", C.c_float),
+        ("block_size", C.c_uint32),
     ]
 
 
@@ -121,6 +122,7 @@ SIGNATURES = {
     "pbf_synchronize": (C.c_int, [_P]),
     "pbf_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
     "pbf_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+    "pbf_autotune": (C.c_int, [_P, C.c_uint32, C.POINTER(Tuning)]),
     "pbf_device_status": (C.c_int, [_P, _U32P]),
     "pbf_enable_timing": (C.c_int, [_P, C.c_int]),
     "pbf_get_timing": (C.c_int, [_P, _F]),
@@ -137,6 +139,7 @@ SIGNATURES = {
     "pbf_backward": (C.c_int, [_P, _P, _P, C.c_int, _P, _P, _P]),
     "pbf_release_record": (C.c_int, [_P]),
     "pbf_status_string": (C.c_char_p, [C.c_int]),
+    "pbf_debug_fail_allocation": (None, [C.c_int]),
     "pbf_last_error": (C.c_char_p, [_P]),
     "pbf_abi_version": (C.c_int, []),
 }

@@ -3,6 +3,7 @@
 // debug reads and the standalone sort / cell-finder entry points.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -144,11 +145,27 @@ pbf_tuning default_tuning() {
     t.use_neighbour_lists = 1;
     t.list_capacity = 128;
     t.skin_h = 0.15f;
+    t.block_size = 256;
     return t;
 }
 
+// Host-side fault injection (pbf_debug_fail_allocation): when armed, the
+// k-th device allocation through dalloc reports cudaErrorMemoryAllocation
+// without touching the device.
+std::atomic<int> g_fail_alloc_after{-1};
+
 template <typename T>
 cudaError_t dalloc(T** p, size_t count) {
+    int k = g_fail_alloc_after.load();
+    while (k >= 0) {
+        if (g_fail_alloc_after.compare_exchange_weak(k, k - 1)) {
+            if (k == 0) {
+                *p = nullptr;
+                return cudaErrorMemoryAllocation;
+            }
+            break;
+        }
+    }
     return cudaMalloc((void**)p, sizeof(T) * (count > 0 ? count : 1));
 }
 
@@ -265,6 +282,7 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
     if (!s->nbr_cnt || s->guard_slots < 2 + s->params.num_solver_iterations)
         return cudaErrorInvalidValue;  // ensure_lists() runs before any capture
     const unsigned g = grid_for(n);
+    const unsigned sb = s->tuning.block_size ? s->tuning.block_size : (unsigned)kBlock;
     const uint32_t iters = s->params.num_solver_iterations;
     cudaStream_t st = s->stream;
     auto mark = [&](uint32_t idx) {
@@ -297,12 +315,12 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
         float4* aux = rec ? rec->AUX[it] : nullptr;
         const int in_slot = it == 0 ? -1 : (int)it;  // displacement of `cur` from XP
         if (it == 0)
-            launch_lambda_build(g, st, s->XP, s->skeys, s->cstart, s->cend, Lk, aux, nl, n, cps);
+            launch_lambda_build(sb, st, s->XP, s->skeys, s->cstart, s->cend, Lk, aux, nl, n, cps);
         else
-            launch_lambda(g, st, cur, s->XP, s->skeys, s->cstart, s->cend, Lk, aux, nl, in_slot, n,
+            launch_lambda(sb, st, cur, s->XP, s->skeys, s->cstart, s->cend, Lk, aux, nl, in_slot, n,
                           cps);
         mark(4 + 2 * it);
-        launch_delta_p(g, st, Lk, s->XP, s->skeys, s->cstart, s->cend, nxt, nl, in_slot,
+        launch_delta_p(sb, st, Lk, s->XP, s->skeys, s->cstart, s->cend, nxt, nl, in_slot,
                        (int)it + 1, n, cps, s->status);
         mark(5 + 2 * it);
         cur = nxt;
@@ -322,11 +340,11 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
     launch_commit(g, st, cur, s->perm, s->x, VS, vort ? nullptr : s->v, n, cps);
     mark(4 + 2 * iters);
     if (vort)
-        launch_vorticity_a(g, st, cur, s->XP, VS, s->skeys, s->cstart, s->cend, s->VX, OM, Q, nl,
+        launch_vorticity_a(sb, st, cur, s->XP, VS, s->skeys, s->cstart, s->cend, s->VX, OM, Q, nl,
                            fin_slot, n, cps);
     mark(5 + 2 * iters);
     if (vort)
-        launch_vorticity_b(g, st, Q, s->XP, s->VX, OM, s->skeys, s->perm, s->cstart, s->cend, s->v,
+        launch_vorticity_b(sb, st, Q, s->XP, s->VX, OM, s->skeys, s->perm, s->cstart, s->cend, s->v,
                            rec ? rec->ETA : nullptr, nl, fin_slot, n, cps);
     mark(6 + 2 * iters);
     return cudaGetLastError();
@@ -533,6 +551,9 @@ pbf_status pbf_set_tuning(pbf_sim* s, const pbf_tuning* t) {
         return fail(s, PBF_ERR_INVALID_ARGUMENT, "list_capacity must be in [1, 4096]");
     if (!(t->skin_h >= 0.0f) || !(t->skin_h <= 1.0f))
         return fail(s, PBF_ERR_INVALID_ARGUMENT, "skin_h must be in [0, 1]");
+    if (t->block_size != 0 && (t->block_size < 32 || t->block_size > (uint32_t)kBlock ||
+                               t->block_size % 32 != 0))
+        return fail(s, PBF_ERR_INVALID_ARGUMENT, "block_size must be 0 or a multiple of 32 in [32, 256]");
     DeviceGuard dg(s->device);
     PBF_CUDA(s, cudaStreamSynchronize(s->stream));
     s->tuning = *t;
@@ -544,6 +565,87 @@ pbf_status pbf_set_tuning(pbf_sim* s, const pbf_tuning* t) {
     invalidate_graph(s);
     PBF_CUDA(s, ensure_lists(s));
     return PBF_OK;
+}
+
+pbf_status pbf_autotune(pbf_sim* s, uint32_t trial_substeps, pbf_tuning* best) {
+    if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
+    if (trial_substeps == 0) return fail(s, PBF_ERR_INVALID_ARGUMENT, "trial_substeps must be positive");
+    DeviceGuard dg(s->device);
+    const size_t b = sizeof(float4) * s->n;
+    float4 *sx = nullptr, *sv = nullptr;
+    PBF_CUDA(s, cudaMalloc(&sx, b));
+    cudaError_t e = cudaMalloc(&sv, b);
+    if (e != cudaSuccess) {
+        cudaFree(sx);
+        return cuda_fail(s, e, "autotune snapshot");
+    }
+    cudaStream_t st = s->stream;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    auto cleanup = [&]() {
+        cudaFree(sx);
+        cudaFree(sv);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    };
+    e = cudaMemcpyAsync(sx, s->x, b, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(sv, s->v, b, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) {
+        cleanup();
+        return cuda_fail(s, e, "autotune snapshot");
+    }
+    const pbf_tuning original = s->tuning;
+    std::vector<pbf_tuning> cand;
+    for (uint32_t blk : {128u, 256u}) {
+        pbf_tuning t = original;
+        t.block_size = blk;
+        t.use_neighbour_lists = 0;
+        cand.push_back(t);
+        for (float skin : {0.05f, 0.1f, 0.2f}) {
+            t.use_neighbour_lists = 1;
+            t.skin_h = skin;
+            if (t.list_capacity == 0) t.list_capacity = 128;
+            cand.push_back(t);
+        }
+    }
+    float best_ms = 1e30f;
+    pbf_tuning best_t = original;
+    pbf_status r = PBF_OK;
+    for (const pbf_tuning& t : cand) {
+        r = pbf_set_tuning(s, &t);
+        if (r != PBF_OK) break;
+        // one untimed substep captures the graph, then the timed trial
+        for (int pass = 0; pass < 2 && r == PBF_OK; ++pass) {
+            cudaMemcpyAsync(s->x, sx, b, cudaMemcpyDeviceToDevice, st);
+            cudaMemcpyAsync(s->v, sv, b, cudaMemcpyDeviceToDevice, st);
+            if (pass == 1) cudaEventRecord(e0, st);
+            r = pbf_step(s, pass == 0 ? 1 : trial_substeps);
+            if (pass == 1) cudaEventRecord(e1, st);
+        }
+        if (r != PBF_OK) break;
+        if ((e = cudaEventSynchronize(e1)) != cudaSuccess) {
+            r = cuda_fail(s, e, "autotune trial");
+            break;
+        }
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best_ms) {
+            best_ms = ms;
+            best_t = t;
+        }
+    }
+    cudaMemcpyAsync(s->x, sx, b, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(s->v, sv, b, cudaMemcpyDeviceToDevice, st);
+    cudaStreamSynchronize(st);
+    cleanup();
+    if (r != PBF_OK) {
+        pbf_set_tuning(s, &original);
+        return r;
+    }
+    r = pbf_set_tuning(s, &best_t);
+    if (r == PBF_OK && best) *best = best_t;
+    return r == PBF_OK ? check_status(s) : r;
 }
 
 pbf_status pbf_get_tuning(const pbf_sim* s, pbf_tuning* out) {
@@ -834,6 +936,8 @@ pbf_status pbf_find_cells(const uint32_t* sorted_keys, uint32_t n, uint32_t num_
     if (hbad) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "a sorted key is >= num_cells");
     return PBF_OK;
 }
+
+void pbf_debug_fail_allocation(int after) { g_fail_alloc_after.store(after < 0 ? -1 : after); }
 
 const char* pbf_last_error(const pbf_sim* s) {
     if (s) return s->err.c_str();

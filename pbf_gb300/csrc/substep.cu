@@ -428,22 +428,22 @@ void launch_keys_of(unsigned g, cudaStream_t st, const float4* x, float4* xstar,
     k_keys_of<CP><<<g, kBlock, 0, st>>>(x, xstar, keys, n, cp);
 }
 template <class CP>
-void launch_lambda_build(unsigned g, cudaStream_t st, const float4* XP, const uint32_t* skeys,
+void launch_lambda_build(unsigned block, cudaStream_t st, const float4* XP, const uint32_t* skeys,
                          const int32_t* cstart, const int32_t* cend, float4* L, float4* aux,
                          NbrLists nl, uint32_t n, CP cp) {
-    k_lambda_build<CP><<<g, kBlock, 0, st>>>(XP, skeys, cstart, cend, L, aux, nl, n, cp);
+    k_lambda_build<CP><<<grid_for(n, (int)block), block, 0, st>>>(XP, skeys, cstart, cend, L, aux, nl, n, cp);
 }
 template <class CP>
-void launch_lambda(unsigned g, cudaStream_t st, const float4* P, const float4* XP,
+void launch_lambda(unsigned block, cudaStream_t st, const float4* P, const float4* XP,
                    const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* L,
                    float4* aux, NbrLists nl, int dmax_slot, uint32_t n, CP cp) {
-    k_lambda<CP><<<g, kBlock, 0, st>>>(P, XP, skeys, cstart, cend, L, aux, nl, dmax_slot, n, cp);
+    k_lambda<CP><<<grid_for(n, (int)block), block, 0, st>>>(P, XP, skeys, cstart, cend, L, aux, nl, dmax_slot, n, cp);
 }
 template <class CP>
-void launch_delta_p(unsigned g, cudaStream_t st, const float4* L, const float4* XP,
+void launch_delta_p(unsigned block, cudaStream_t st, const float4* L, const float4* XP,
                     const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* Pn,
                     NbrLists nl, int dmax_slot, int out_slot, uint32_t n, CP cp, uint32_t* status) {
-    k_delta_p<CP><<<g, kBlock, 0, st>>>(L, XP, skeys, cstart, cend, Pn, nl, dmax_slot, out_slot, n,
+    k_delta_p<CP><<<grid_for(n, (int)block), block, 0, st>>>(L, XP, skeys, cstart, cend, Pn, nl, dmax_slot, out_slot, n,
                                         cp, status);
 }
 template <class CP>
@@ -452,20 +452,20 @@ void launch_commit(unsigned g, cudaStream_t st, const float4* P, const uint32_t*
     k_commit<CP><<<g, kBlock, 0, st>>>(P, perm, x, VS, v_out, n, cp);
 }
 template <class CP>
-void launch_vorticity_a(unsigned g, cudaStream_t st, const float4* P, const float4* XP,
+void launch_vorticity_a(unsigned block, cudaStream_t st, const float4* P, const float4* XP,
                         const float4* VS, const uint32_t* skeys, const int32_t* cstart,
                         const int32_t* cend, float4* VX, float4* OM, float4* Q, NbrLists nl,
                         int dmax_slot, uint32_t n, CP cp) {
-    k_vorticity_a<CP><<<g, kBlock, 0, st>>>(P, XP, VS, skeys, cstart, cend, VX, OM, Q, nl,
+    k_vorticity_a<CP><<<grid_for(n, (int)block), block, 0, st>>>(P, XP, VS, skeys, cstart, cend, VX, OM, Q, nl,
                                             dmax_slot, n, cp);
 }
 template <class CP>
-void launch_vorticity_b(unsigned g, cudaStream_t st, const float4* Q, const float4* XP,
+void launch_vorticity_b(unsigned block, cudaStream_t st, const float4* Q, const float4* XP,
                         const float4* VX, const float4* OM, const uint32_t* skeys,
                         const uint32_t* perm, const int32_t* cstart, const int32_t* cend,
                         float4* v, float4* eta_out, NbrLists nl, int dmax_slot, uint32_t n,
                         CP cp) {
-    k_vorticity_b<CP><<<g, kBlock, 0, st>>>(Q, XP, VX, OM, skeys, perm, cstart, cend, v, eta_out,
+    k_vorticity_b<CP><<<grid_for(n, (int)block), block, 0, st>>>(Q, XP, VX, OM, skeys, perm, cstart, cend, v, eta_out,
                                             nl, dmax_slot, n, cp);
 }
 template <class CP>

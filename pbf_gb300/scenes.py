@@ -164,3 +164,17 @@ def batch_scenes(num_scenes: int = 256, seed: int = 7, iterations: int = 4, subs
 def concat_state(scenes_: list[Scene]):
     return (np.ascontiguousarray(np.concatenate([s.x4 for s in scenes_])),
             np.ascontiguousarray(np.concatenate([s.v4 for s in scenes_])))
+
+
+def shard(scenes_: list[Scene], rank: int, world: int) -> list[int]:
+    """Indices of the scenes rank `rank` of `world` steps when a batch is split
+    across GPUs (independent scenes need no exchange): greedy by particle
+    count, largest first, so every rank gets a near-equal share."""
+    order = sorted(range(len(scenes_)), key=lambda k: -scenes_[k].n)
+    load = [0] * world
+    owner = [0] * len(scenes_)
+    for k in order:
+        r = min(range(world), key=lambda q: (load[q], q))
+        owner[k] = r
+        load[r] += scenes_[k].n
+    return [k for k in range(len(scenes_)) if owner[k] == rank]

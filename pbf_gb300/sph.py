@@ -168,7 +168,8 @@ class SPH:
         check(self._lib.pbf_get_tuning(self._h, C.byref(t)), self._h)
         return t
 
-    def set_tuning(self, use_neighbour_lists=None, list_capacity=None, skin_h=None) -> None:
+    def set_tuning(self, use_neighbour_lists=None, list_capacity=None, skin_h=None,
+                   block_size=None) -> None:
         t = self.get_tuning()
         if use_neighbour_lists is not None:
             t.use_neighbour_lists = 1 if use_neighbour_lists else 0
@@ -176,7 +177,15 @@ class SPH:
             t.list_capacity = int(list_capacity)
         if skin_h is not None:
             t.skin_h = float(skin_h)
+        if block_size is not None:
+            t.block_size = int(block_size)
         check(self._lib.pbf_set_tuning(self._h, C.byref(t)), self._h)
+
+    def autotune(self, trial_substeps: int = 10) -> dict:
+        """Picks the fastest tuning for the current state (pbf_autotune)."""
+        t = Tuning()
+        check(self._lib.pbf_autotune(self._h, int(trial_substeps), C.byref(t)), self._h)
+        return {name: getattr(t, name) for name, _ in Tuning._fields_}
 
     # ---- state ------------------------------------------------------------
     def set_state(self, x4, v4) -> None:

@@ -253,3 +253,45 @@ def test_lists_exact_in_a_calm_scene(gpu, oracle_mod):
     ox, ov = o.get_state()
     assert_bits(x, ox, "positions after 60 calm substeps")
     assert_bits(v, ov, "velocities after 60 calm substeps")
+
+
+def test_block_size_and_autotune_never_change_results(gpu, oracle_mod):
+    sc = scenes.plain_16k()
+    o = run_oracle(oracle_mod, sc.params, sc.x4, sc.v4, 12)
+    ox, ov = o.get_state()
+    for blk in (32, 128, 256):
+        g = pg.SPH(sc.n, tuple(sc.params.grid), sc.params)
+        g.set_tuning(block_size=blk)
+        g.set_state(sc.x4, sc.v4)
+        g.step(12)
+        assert_bits(g.positions(), ox, f"positions with block {blk}")
+    g = pg.SPH(sc.n, tuple(sc.params.grid), sc.params)
+    g.set_state(sc.x4, sc.v4)
+    best = g.autotune(4)
+    assert best["block_size"] in (128, 256)
+    # the autotuner leaves the state where it was
+    assert np.array_equal(g.positions(), sc.x4)
+    g.step(12)
+    x, v = g.get_state()
+    assert_bits(x, ox, "positions after autotune")
+    assert_bits(v, ov, "velocities after autotune")
+    with pytest.raises(pg.PbfError):
+        g.set_tuning(block_size=48)
+
+
+@pytest.mark.parametrize("after", [0, 1, 5, 12, 16])
+def test_allocation_failure_is_reported_and_cleaned_up(gpu, after):
+    """Host-side fault injection: the k-th device allocation reports out of
+    memory; creation fails with PBF_ERR_OUT_OF_MEMORY, frees what it got, and
+    the next creation works."""
+    sc = scenes.plain_16k()
+    lib = pg.load()
+    lib.pbf_debug_fail_allocation(after)
+    try:
+        with pytest.raises(pg.PbfError) as e:
+            pg.SPH(sc.n, tuple(sc.params.grid), sc.params)
+        assert e.value.status == 2
+    finally:
+        lib.pbf_debug_fail_allocation(-1)
+    g = run_gpu(sc.params, sc.x4, sc.v4, 1)
+    assert np.all(np.isfinite(g.positions()))
