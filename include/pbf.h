@@ -312,6 +312,21 @@ pbf_status pbf_backward(pbf_sim* sim, const float* dL_dx4, const float* dL_dv4, 
 /* Frees the recording of pbf_forward_record. */
 pbf_status pbf_release_record(pbf_sim* sim);
 
+/* SPH's highlight pass (clearhighlight.glsl:7, highlight.glsl:16-30, run from
+ * src/SPH.cpp:288-297): flags (one uint32 per particle, id order) have bit 0
+ * set on selected particles; bit 1 is cleared everywhere and then set on every
+ * stencil candidate of a selected particle (the 27-cell candidates, as the
+ * reference's FOR_EACH_NEIGHBOUR, not distance-filtered), using the last
+ * substep's sort.  Synchronising. */
+pbf_status pbf_highlight_neighbours(pbf_sim* sim, uint32_t* flags, int where);
+
+/* Binary snapshot of the state (no reference counterpart: the reference only
+ * resets to its initial blocks, src/Simulation.cpp:303-305): "PBFSTATE",
+ * u32 version 1, u32 particle count, u32 scene count, u32 0, then x and v as
+ * float4[n] in id order, little-endian.  Loading checks the particle count. */
+pbf_status pbf_save_state(pbf_sim* sim, const char* path);
+pbf_status pbf_load_state(pbf_sim* sim, const char* path);
+
 /* ---- diagnostics ------------------------------------------------------------- */
 
 typedef struct pbf_diagnostics {

@@ -69,6 +69,7 @@ def load() -> C.CDLL:
         lib.pbfo_get_consts.argtypes = [P, P]
         lib.pbfo_diagnostics.argtypes = [P, P]
         lib.pbfo_radix_sort.argtypes = [P, C.c_uint32, C.c_uint32, P, P]
+        lib.pbfo_highlight.argtypes = [P, P]
         lib.pbfo_max_threads.restype = C.c_int
         lib.pbfo_sample_substep.restype = C.c_double
         lib.pbfo_sample_substep.argtypes = [P, C.c_uint32, C.c_uint32, P, P]
@@ -147,6 +148,13 @@ class Oracle:
         self._lib.pbfo_get_runs(self._h, int(i), r.ctypes.data)
         return r.reshape(9, 2)
 
+    def highlight(self, flags):
+        """Highlight pass over the last substep's runs (see pbfo_highlight)."""
+        f = np.ascontiguousarray(flags, np.uint32).copy()
+        assert f.shape == (self.n,)
+        self._lib.pbfo_highlight(self._h, f.ctypes.data)
+        return f
+
     def consts(self):
         out = np.empty(4, np.float64)
         self._lib.pbfo_get_consts(self._h, out.ctypes.data)
@@ -205,14 +213,18 @@ def ref_load() -> C.CDLL:
         P = C.c_void_p
         lib.pbfr_substep.argtypes = [P, C.c_uint32, P, P, P, P, P, P, P]
         lib.pbfr_substep.restype = C.c_int
+        lib.pbfr_substep_highlight.argtypes = [P, C.c_uint32, P, P, P, P, P, P, P, P]
+        lib.pbfr_substep_highlight.restype = C.c_int
         _ref = lib
     return _ref
 
 
-def ref_substep(params, x4, v4):
+def ref_substep(params, x4, v4, highlight=None):
     """One SPH::Run of the reference's shaders.  Returns a dict with x, v (id
     order), sorted ids, the grid start/end textures (x fastest, then y, z),
-    the packed neighbour texture (n, 3, 4) and lambda (sorted order)."""
+    the packed neighbour texture (n, 3, 4) and lambda (sorted order); with
+    `highlight` (uint32[n] flags, id order) also the flags after the
+    clearhighlight / highlight dispatches of that substep."""
     lib = ref_load()
     n = x4.shape[0]
     x = np.ascontiguousarray(x4, np.float32).copy()
@@ -224,7 +236,12 @@ def ref_substep(params, x4, v4):
     en = np.empty(cells, np.int32)
     nbr = np.empty(12 * n, np.int32)
     lam = np.empty(n, np.float32)
-    lib.pbfr_substep(C.addressof(params), n, x.ctypes.data, v.ctypes.data, ids.ctypes.data,
-                     st.ctypes.data, en.ctypes.data, nbr.ctypes.data, lam.ctypes.data)
-    return {"x": x, "v": v, "ids": ids, "start": st.reshape(g[2], g[1], g[0]),
+    hl = None
+    if highlight is not None:
+        hl = np.ascontiguousarray(highlight, np.uint32).copy()
+        assert hl.shape == (n,)
+    lib.pbfr_substep_highlight(C.addressof(params), n, x.ctypes.data, v.ctypes.data,
+                               ids.ctypes.data, st.ctypes.data, en.ctypes.data, nbr.ctypes.data,
+                               lam.ctypes.data, None if hl is None else hl.ctypes.data)
+    return {"highlight": hl, "x": x, "v": v, "ids": ids, "start": st.reshape(g[2], g[1], g[0]),
             "end": en.reshape(g[2], g[1], g[0]), "nbr": nbr.reshape(n, 3, 4), "lambda": lam}

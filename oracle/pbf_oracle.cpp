@@ -147,6 +147,22 @@ void pbfo_get_runs(void* hp, uint32_t i, int32_t* runs) {
     }
 }
 
+// clearhighlight.glsl:7 then highlight.glsl:16-30 over the last substep's
+// runs: bit 1 cleared, then set on every stencil candidate (j != i) of a
+// particle whose bit 0 is set.  flags[n] in id order.
+void pbfo_highlight(void* hp, uint32_t* flags) {
+    Handle* h = (Handle*)hp;
+    auto run = [&](auto& s) {
+        for (uint32_t i = 0; i < s.n; ++i) flags[i] &= 1u;
+        for (uint32_t i = 0; i < s.n; ++i)
+            if (flags[s.perm[i]] & 1u) s.for_each_neighbour(i, [&](uint32_t j) { flags[s.perm[j]] |= 2u; });
+    };
+    if (h->fp64)
+        run(h->d);
+    else
+        run(h->f);
+}
+
 // The folded constants (k6, kg, kg_lambda, h2) as doubles, for tests.
 void pbfo_get_consts(void* hp, double* out4) {
     Handle* h = (Handle*)hp;

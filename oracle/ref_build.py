@@ -13,7 +13,8 @@ GLSL float literals float and `-ffp-contract=off` one rounding per operation.
 The generated file and the library go to oracle/_ref/ (git-ignored).
 
 Shaders used (SPH::Run, src/SPH.cpp:246-334): sph/predictpos, sph/calclambda,
-sph/updatepos, sph/update, sph/vorticity (each prefixed with
+sph/updatepos, sph/update, sph/vorticity, sph/clearhighlight, sph/highlight
+(each prefixed with
 sph/foreachneighbour, as SPH's constructor compiles them, src/SPH.cpp:63-90),
 neighbourcellfinder/findcells and neighbourcells, and GetHash from
 radixsort/counting.  The radix sort's counting / blockscan / addblocksum /
@@ -33,7 +34,8 @@ OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT, "libpbf_ref.so")
 SHIM = os.path.join(HERE, "ref_shim")
 
-SPH_SHADERS = ["predictpos", "calclambda", "updatepos", "update", "vorticity"]
+SPH_SHADERS = ["predictpos", "calclambda", "updatepos", "update", "vorticity", "clearhighlight",
+               "highlight"]
 NCF_SHADERS = ["findcells", "neighbourcells"]
 
 

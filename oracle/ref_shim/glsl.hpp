@@ -107,6 +107,9 @@ struct ivec4 {
 struct uvec3 {
     uint x, y, z;
 };
+struct uvec4 {
+    uint x, y, z, w;
+};
 
 inline float dot(vec3 a, vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 // GLSL has no integer dot: ivec3 arguments convert to vec3 implicitly, so
@@ -158,6 +161,10 @@ struct iimageBuffer {
     int* data = nullptr;
 };
 
+struct uimageBuffer {  // r32ui
+    uint* data = nullptr;
+};
+
 inline vec4 texelFetch(const samplerBuffer& t, int i) {
     if (t.lanes == 1) return vec4(t.data[i], 0.0f, 0.0f, 1.0f);
     return vec4(t.data[4 * i], t.data[4 * i + 1], t.data[4 * i + 2], t.data[4 * i + 3]);
@@ -193,6 +200,19 @@ inline void imageStore(iimageBuffer& im, int i, ivec4 v) {
     im.data[4 * i + 1] = v.y;
     im.data[4 * i + 2] = v.z;
     im.data[4 * i + 3] = v.w;
+}
+
+inline uvec4 imageLoad(const uimageBuffer& im, int i) { return uvec4{im.data[i], 0u, 0u, 1u}; }
+// invocations run one after another, so the atomics are plain read-modify-writes
+inline uint imageAtomicOr(uimageBuffer& im, int i, uint v) {
+    const uint old = im.data[i];
+    im.data[i] = old | v;
+    return old;
+}
+inline uint imageAtomicAnd(uimageBuffer& im, int i, uint v) {
+    const uint old = im.data[i];
+    im.data[i] = old & v;
+    return old;
 }
 
 inline void barrier() {}

@@ -72,9 +72,12 @@ int pbfr_record_size(void) { return (int)sizeof(Rec); }
 // outputs: sorted ids [n], grid start/end textures [Gx*Gy*Gz] (x fastest,
 // then y, then z: the 3-D texture layout), the packed neighbour texture
 // [12 n] (start | count << 24, 3 ivec4 per sorted particle), lambda of the
-// last iteration [n] (sorted).
-int pbfr_substep(const Params* p, uint32_t n, float* x4, float* v4, uint32_t* out_ids,
-                 int32_t* out_start, int32_t* out_end, int32_t* out_nbr, float* out_lambda) {
+// last iteration [n] (sorted).  highlight (uint32[n], id order, may be NULL)
+// goes through the clearhighlight and highlight dispatches, which SPH::Run
+// issues after the neighbour search (src/SPH.cpp:288-297).
+int pbfr_substep_highlight(const Params* p, uint32_t n, float* x4, float* v4, uint32_t* out_ids,
+                           int32_t* out_start, int32_t* out_end, int32_t* out_nbr,
+                           float* out_lambda, uint32_t* highlight) {
     using namespace glsl;
     namespace G = refglobals;
     const int gx = (int)p->grid[0], gy = (int)p->grid[1], gz = (int)p->grid[2];
@@ -131,6 +134,23 @@ int pbfr_substep(const Params* p, uint32_t n, float* x4, float* v4, uint32_t* ou
     for (uint32_t g = 0; g < n; ++g) {
         set_invocation(g);
         sh_neighbourcells::main_invocation();
+    }
+
+    // particle highlighting (each invocation's atomics land at once; the
+    // highlight shader only reads bit 0, which no invocation changes)
+    if (highlight) {
+        sh_clearhighlight::highlighttexture = uimageBuffer{highlight};
+        for (uint32_t g = 0; g < n; ++g) {
+            set_invocation(g);
+            sh_clearhighlight::main_invocation();
+        }
+        sh_highlight::particlekeys = reinterpret_cast<sh_highlight::ParticleKey*>(sorted.data());
+        sh_highlight::neighbourcelltexture = isamplerBuffer{nbr.data()};
+        sh_highlight::highlighttexture = uimageBuffer{highlight};
+        for (uint32_t g = 0; g < n; ++g) {
+            set_invocation(g);
+            sh_highlight::main_invocation();
+        }
     }
 
     // 4 solver iterations
@@ -195,6 +215,12 @@ int pbfr_substep(const Params* p, uint32_t n, float* x4, float* v4, uint32_t* ou
     if (out_nbr) std::copy(nbr.begin(), nbr.end(), out_nbr);
     if (out_lambda) std::copy(lambda.begin(), lambda.end(), out_lambda);
     return 0;
+}
+
+int pbfr_substep(const Params* p, uint32_t n, float* x4, float* v4, uint32_t* out_ids,
+                 int32_t* out_start, int32_t* out_end, int32_t* out_nbr, float* out_lambda) {
+    return pbfr_substep_highlight(p, n, x4, v4, out_ids, out_start, out_end, out_nbr, out_lambda,
+                                  nullptr);
 }
 
 }  // extern "C"

@@ -937,6 +937,66 @@ pbf_status pbf_find_cells(const uint32_t* sorted_keys, uint32_t n, uint32_t num_
     return PBF_OK;
 }
 
+pbf_status pbf_highlight_neighbours(pbf_sim* s, uint32_t* flags, int where) {
+    if (!s || !flags) return fail(s, PBF_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (where != PBF_HOST && where != PBF_DEVICE) return fail(s, PBF_ERR_INVALID_ARGUMENT, "bad where");
+    DeviceGuard dg(s->device);
+    cudaStream_t st = s->stream;
+    const size_t b = sizeof(uint32_t) * s->n;
+    uint32_t* d = flags;
+    if (where == PBF_HOST) {
+        PBF_CUDA(s, cudaMallocAsync((void**)&d, b, st));
+        PBF_CUDA(s, cudaMemcpyAsync(d, flags, b, cudaMemcpyHostToDevice, st));
+    }
+    const unsigned g = grid_for(s->n);
+    // the sorted particle's scene for batches comes from the sorted scene ids
+    if (s->nscenes == 1)
+        launch_highlight(g, st, s->skeys, s->perm, s->cstart, s->cend, d, s->n, OneScene{s->dc});
+    else
+        launch_highlight(g, st, s->skeys, s->perm, s->cstart, s->cend, d, s->n,
+                         ManyScenes{s->d_consts, s->sid_sorted});
+    PBF_CUDA(s, cudaGetLastError());
+    if (where == PBF_HOST) {
+        PBF_CUDA(s, cudaMemcpyAsync(flags, d, b, cudaMemcpyDeviceToHost, st));
+        PBF_CUDA(s, cudaFreeAsync(d, st));
+    }
+    return check_status(s);
+}
+
+// Snapshot file: "PBFSTATE" magic, u32 format version 1, u32 particle count,
+// u32 scene count, u32 reserved, then x and v as float4[n] (id order),
+// little-endian.
+pbf_status pbf_save_state(pbf_sim* s, const char* path) {
+    if (!s || !path) return fail(s, PBF_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::vector<float> x(4ull * s->n), v(4ull * s->n);
+    pbf_status r = pbf_get_state(s, x.data(), v.data(), PBF_HOST);
+    if (r != PBF_OK) return r;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(s, PBF_ERR_INVALID_ARGUMENT, std::string("cannot open ") + path);
+    const uint32_t hdr[4] = {1u, s->n, s->nscenes, 0u};
+    bool ok = std::fwrite("PBFSTATE", 1, 8, f) == 8 && std::fwrite(hdr, 4, 4, f) == 4 &&
+              std::fwrite(x.data(), 4, x.size(), f) == x.size() &&
+              std::fwrite(v.data(), 4, v.size(), f) == v.size();
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? PBF_OK : fail(s, PBF_ERR_INVALID_ARGUMENT, std::string("cannot write ") + path);
+}
+
+pbf_status pbf_load_state(pbf_sim* s, const char* path) {
+    if (!s || !path) return fail(s, PBF_ERR_INVALID_ARGUMENT, "NULL argument");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(s, PBF_ERR_INVALID_ARGUMENT, std::string("cannot open ") + path);
+    char magic[8];
+    uint32_t hdr[4];
+    std::vector<float> x(4ull * s->n), v(4ull * s->n);
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "PBFSTATE", 8) == 0 &&
+              std::fread(hdr, 4, 4, f) == 4 && hdr[0] == 1u && hdr[1] == s->n &&
+              std::fread(x.data(), 4, x.size(), f) == x.size() &&
+              std::fread(v.data(), 4, v.size(), f) == v.size() && std::fgetc(f) == EOF;
+    std::fclose(f);
+    if (!ok) return fail(s, PBF_ERR_INVALID_ARGUMENT, std::string("not a snapshot of this handle: ") + path);
+    return pbf_set_state(s, x.data(), v.data(), PBF_HOST);
+}
+
 void pbf_debug_fail_allocation(int after) { g_fail_alloc_after.store(after < 0 ? -1 : after); }
 
 const char* pbf_last_error(const pbf_sim* s) {

@@ -415,6 +415,45 @@ k_diagnostics(const float4* __restrict__ P, const float4* __restrict__ v,
                          0.5f * (w.x * w.x + w.y * w.y + w.z * w.z), (float)cand, 0.0f);
 }
 
+// highlight.glsl:16-30 after clearhighlight.glsl: bit 1 of every particle is
+// cleared, then set on all stencil candidates (not distance-filtered, as the
+// reference's FOR_EACH_NEIGHBOUR) of each particle whose bit 0 is set.
+// flags are in id order; the candidates come from the last substep's sort.
+template <class CP>
+__global__ void __launch_bounds__(kBlock)
+k_highlight(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
+            const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
+            uint32_t* flags, uint32_t n, CP cp) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t id = perm[i];
+    if (id >= n || (flags[id] & 1u) == 0u) return;
+    const auto& c = cp.at(i);
+    visit_full(i, skeys[i], c, cstart, cend, [&](uint32_t j) {
+        const uint32_t pj = perm[j];
+        if (pj < n) atomicOr(flags + pj, 2u);
+    });
+}
+
+__global__ void __launch_bounds__(kBlock) k_clear_highlight(uint32_t* flags, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) flags[i] &= 1u;  // clearhighlight.glsl:7
+}
+
+template <class CP>
+void launch_highlight(unsigned g, cudaStream_t st, const uint32_t* skeys, const uint32_t* perm,
+                      const int32_t* cstart, const int32_t* cend, uint32_t* flags, uint32_t n,
+                      CP cp) {
+    k_clear_highlight<<<g, kBlock, 0, st>>>(flags, n);
+    k_highlight<CP><<<g, kBlock, 0, st>>>(skeys, perm, cstart, cend, flags, n, cp);
+}
+template void launch_highlight<OneScene>(unsigned, cudaStream_t, const uint32_t*, const uint32_t*,
+                                         const int32_t*, const int32_t*, uint32_t*, uint32_t,
+                                         OneScene);
+template void launch_highlight<ManyScenes>(unsigned, cudaStream_t, const uint32_t*,
+                                           const uint32_t*, const int32_t*, const int32_t*,
+                                           uint32_t*, uint32_t, ManyScenes);
+
 // Host-side launchers: the template kernels are launched from this file
 // (their host stubs are not visible to other translation units).
 template <class CP>

@@ -55,4 +55,9 @@ void launch_diagnostics(unsigned g, cudaStream_t st, const float4* P, const floa
                         const uint32_t* skeys, const uint32_t* perm, const int32_t* cstart,
                         const int32_t* cend, float4* out, uint32_t n, CP cp);
 
+template <class CP>
+void launch_highlight(unsigned g, cudaStream_t st, const uint32_t* skeys, const uint32_t* perm,
+                      const int32_t* cstart, const int32_t* cend, uint32_t* flags, uint32_t n,
+                      CP cp);
+
 }  // namespace pbf

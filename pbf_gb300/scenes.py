@@ -178,3 +178,32 @@ def shard(scenes_: list[Scene], rank: int, world: int) -> list[int]:
         owner[k] = r
         load[r] += scenes_[k].n
     return [k for k in range(len(scenes_)) if owner[k] == rank]
+
+
+def reference_two_blocks(seed: int = 0) -> Scene:
+    """The reference application's own scene (Simulation::ResetParticleBuffer,
+    src/Simulation.cpp:206-246, with SPH's defaults, src/SPH.cpp:24-26,136-144):
+    65,536 particles in two 32^3 blocks of spacing 0.94, one from
+    (32.5, 0.5, 32.5) along +x, +y, +z and one from (95.5, 0.5, 95.5) along
+    -x, +y, -z, each coordinate jittered by 0.01 * (U(0,1) - 0.5) (the
+    reference's unseeded rand(); here a seeded generator), zero velocities, in
+    the (128, 64, 128) grid with the reference's walls, h = 2 and 5 solver
+    iterations, vorticity confinement off."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    blocks = []
+    for origin, sign in (((32.5, 0.5, 32.5), (1, 1, 1)), ((95.5, 0.5, 95.5), (-1, 1, -1))):
+        # id order x outermost, then z, then y (src/Simulation.cpp:214-229)
+        gi, gk, gj = np.meshgrid(np.arange(32), np.arange(32), np.arange(32), indexing="ij")
+        idx = np.stack([gi.ravel(), gj.ravel(), gk.ravel()], 1).astype(np.float64)
+        pos = np.asarray(origin) + 0.94 * idx * np.asarray(sign, np.float64)
+        pos += 0.01 * (rng.random(pos.shape) - 0.5)
+        blocks.append(pos)
+    pos = np.concatenate(blocks)
+    x4 = np.zeros((pos.shape[0], 4), np.float32)
+    x4[:, :3] = pos.astype(np.float32)
+    v4 = np.zeros_like(x4)
+    from .sph import default_params
+    p = default_params((128, 64, 128))
+    p.h = 2.0
+    p.tensile_instability_scale = float(np.float32(1.0 / wpoly6(0.2, 2.0)))
+    return Scene("reference_two_blocks", p, x4, v4, 0, {"seed": seed})

@@ -224,6 +224,39 @@ class SPH:
         check(self._lib.pbf_device_buffers(self._h, None, C.byref(v)), self._h)
         return int(v.value)
 
+    def save_state(self, path: str) -> None:
+        """Binary snapshot of x, v (pbf_save_state)."""
+        check(self._lib.pbf_save_state(self._h, str(path).encode()), self._h)
+
+    def load_state(self, path: str) -> None:
+        check(self._lib.pbf_load_state(self._h, str(path).encode()), self._h)
+
+    def highlight_flags(self, flags) -> None:
+        """The highlight pass on a flag buffer (the reference's highlight
+        buffer, src/SPH.h:201-207), updated in place: a uint32 numpy array, or
+        a contiguous int32/uint32 CUDA tensor on this handle's device.  Bit 0
+        marks selected particles; bit 1 is cleared and set on every stencil
+        candidate of a selected particle, from the last substep's sort."""
+        if isinstance(flags, np.ndarray):
+            if flags.dtype != np.uint32 or flags.shape != (self._n,) or not flags.flags.c_contiguous:
+                raise ValueError("flags must be a contiguous uint32 array of one entry per particle")
+            check(self._lib.pbf_highlight_neighbours(self._h, flags.ctypes.data, PBF_HOST), self._h)
+            return
+        import torch
+        if not (isinstance(flags, torch.Tensor) and flags.is_cuda and flags.is_contiguous()
+                and flags.numel() == self._n and flags.element_size() == 4):
+            raise ValueError("flags must be a contiguous 4-byte CUDA tensor of one entry per particle")
+        torch.cuda.current_stream(flags.device).synchronize()
+        check(self._lib.pbf_highlight_neighbours(self._h, flags.data_ptr(), PBF_DEVICE), self._h)
+
+    def highlight_neighbours(self, selected) -> np.ndarray:
+        """Flags with bit 0 on the `selected` ids and bit 1 on their stencil
+        candidates in the last substep."""
+        flags = np.zeros(self._n, np.uint32)
+        flags[np.asarray(selected, np.int64)] = 1
+        self.highlight_flags(flags)
+        return flags
+
     # ---- stepping -----------------------------------------------------------
     def Run(self) -> None:
         """One substep (SPH::Run, src/SPH.cpp:246-334); asynchronous."""

@@ -24,10 +24,11 @@ def main():
     manifest = {}
     for name in pin_scenes.CASES:
         p, x4, v4 = pin_scenes.make(name)
-        r = oracle.ref_substep(p, x4, v4)
+        hl_in = pin_scenes.highlight_flags(x4.shape[0])
+        r = oracle.ref_substep(p, x4, v4, highlight=hl_in)
         path = os.path.join(HERE, f"ref_{name}.npz")
         np.savez_compressed(path, x_in=x4, v_in=v4, x=r["x"], v=r["v"], ids=r["ids"],
-                            lam=r["lambda"])
+                            lam=r["lambda"], hl_in=hl_in, hl=r["highlight"])
         manifest[os.path.basename(path)] = hashlib.sha256(open(path, "rb").read()).hexdigest()
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py",

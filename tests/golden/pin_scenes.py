@@ -34,3 +34,14 @@ def make(name):
     d = np.array([[0.5, 0.5, 0.5, 0], [GRID - 0.5, GRID - 0.5, GRID - 0.5, 0]], np.float32)
     z = np.zeros((1, 4), np.float32)
     return p, np.concatenate([d[:1], x4, d[1:]]), np.concatenate([z, v4, z])
+
+
+def highlight_flags(n):
+    """Highlight input: bit 0 (selected) on every 395th particle, stale bits 1
+    and 2 elsewhere, which the clear pass must drop."""
+    i = np.arange(n)
+    f = np.zeros(n, np.uint32)
+    f[i % 395 == 5] |= 1
+    f[i % 5 == 0] |= 2
+    f[i % 11 == 0] |= 4
+    return f

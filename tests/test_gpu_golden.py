@@ -33,3 +33,15 @@ def test_gpu_matches_reference_golden(gpu, name):
     assert np.max(np.abs(v[:, :3] - g["v"][:, :3])) <= 1e-5 * h / dt
     if p.num_solver_iterations:
         assert np.max(np.abs(lam - g["lam"])) <= 2e-5
+
+
+@pytest.mark.parametrize("name", list(pin_scenes.CASES))
+def test_gpu_highlight_matches_reference_golden(gpu, name):
+    p, x4, v4 = pin_scenes.make(name)
+    g = np.load(os.path.join(HERE, f"ref_{name}.npz"))
+    sim = pg.SPH(x4.shape[0], tuple(p.grid), p)
+    sim.set_state(x4, v4)
+    sim.step(1)
+    flags = g["hl_in"].copy()
+    sim.highlight_flags(flags)
+    assert np.array_equal(flags, g["hl"])

@@ -64,6 +64,21 @@ def test_oracle_matches_reference_golden(oracle_mod, name):
         assert np.max(np.abs(lam - g["lam"])) <= tol["lam"]
 
 
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_highlight_matches_reference_golden(oracle_mod, name):
+    """clearhighlight + highlight (src/SPH.cpp:288-297) after one substep:
+    identical flags."""
+    p, x4, v4 = pin_scenes.make(name)
+    g = golden(name)
+    assert np.array_equal(g["hl_in"], pin_scenes.highlight_flags(x4.shape[0]))
+    o = oracle_mod.Oracle(p, x4.shape[0])
+    o.set_state(x4, v4)
+    o.step(1)
+    hl = o.highlight(g["hl_in"])
+    assert np.array_equal(hl, g["hl"])
+    assert 0 < int(((hl >> 1) & 1).sum()) < x4.shape[0] // 2  # a real selection, not all or none
+
+
 @pytest.mark.skipif(not oracle.ref_available(), reason="the reference checkout is not on this machine")
 @pytest.mark.parametrize("name", CASES)
 def test_oracle_matches_live_reference_shaders(oracle_mod, name):
@@ -88,6 +103,20 @@ def test_oracle_matches_live_reference_shaders(oracle_mod, name):
             rs, re_ = (0, 0) if pk == -1 else (pk & 0xFFFFFF, (pk & 0xFFFFFF) + (pk >> 24))
             b, e = (int(v) for v in runs[row])
             assert (rs, re_) == (b, e) or (b == e and rs == re_), (i, row, (rs, re_), (b, e))
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="the reference checkout is not on this machine")
+def test_highlight_matches_live_reference_shaders(oracle_mod):
+    """A dense random selection on a violent scene, through the reference's
+    highlight shaders and the oracle."""
+    p, x4, v4 = pin_scenes.make("h1_eps0.01")
+    rng = np.random.default_rng(5)
+    f = rng.integers(0, 8, x4.shape[0]).astype(np.uint32)
+    r = oracle_mod.ref_substep(p, x4, v4, highlight=f)
+    o = oracle_mod.Oracle(p, x4.shape[0])
+    o.set_state(x4, v4)
+    o.step(1)
+    assert np.array_equal(o.highlight(f), r["highlight"])
 
 
 @pytest.mark.skipif(not oracle.ref_available(), reason="the reference checkout is not on this machine")
