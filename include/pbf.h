@@ -184,22 +184,38 @@ typedef struct pbf_tuning {
                                      particle's candidates within h + skin (in the
                                      reference's visit order) and later sweeps replay
                                      them while a displacement guard proves no other
-                                     candidate can be within h; 0: every sweep scans the
-                                     full 27-cell stencil (the reference's loop) */
+                                     candidate can be within h; 0 (default): every
+                                     scanning sweep walks the full 27-cell stencil (the
+                                     reference's loop) */
     uint32_t list_capacity;       /* entries per particle; longer lists fall back to the
                                      full stencil scan for that particle */
     float skin_h;                 /* list radius is h * (1 + skin_h) */
     uint32_t block_size;          /* threads per block of the neighbour sweeps: a
                                      multiple of 32 in [32, 256]; 0 = 256 */
+    uint32_t sweep_mode;          /* PBF_SWEEP_DIRECT: a full stencil scan evaluates each
+                                     candidate within h where it finds it;
+                                     PBF_SWEEP_MASKED (default): it scans each run in
+                                     chunks of 32 candidates, marks the ones within h in
+                                     a bit mask, then evaluates the marked ones, in the
+                                     same order (a warp's lanes stay converged) */
+    uint32_t pair_list_capacity;  /* > 0: each lambda sweep records every particle's
+                                     candidates within h (in visit order, up to this
+                                     many) and the delta-p sweep over the same positions
+                                     replays them instead of scanning the stencil; the
+                                     same between the two vorticity passes.  Longer
+                                     lists fall back to the scan.  0 = off; default 64 */
 } pbf_tuning;
+
+enum { PBF_SWEEP_DIRECT = 0, PBF_SWEEP_MASKED = 1 };
 
 /* No reference counterpart (the reference has no tuning surface). */
 pbf_status pbf_set_tuning(pbf_sim* sim, const pbf_tuning* tuning);
 pbf_status pbf_get_tuning(const pbf_sim* sim, pbf_tuning* out);
 
 /* Autotuner: times `trial_substeps` substeps from the current state under
- * each candidate tuning (sweep block size 128 / 256; neighbour lists off, or
- * on with skin 0.05h / 0.1h / 0.2h), restoring the state before every trial
+ * each candidate tuning (sweep block size 128 / 256; direct or masked
+ * sweeps; neighbour lists off, or on with skin 0.05h / 0.1h / 0.2h),
+ * restoring the state before every trial
  * and after the last, and keeps the fastest, which it also writes to `best`
  * (may be NULL).  The state is unchanged on return.  Since no tuning changes
  * any result, tuning never changes a simulation. */

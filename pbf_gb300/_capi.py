@@ -69,6 +69,8 @@ class Tuning(C.Structure):
         ("list_capacity", C.c_uint32),
         ("skin_h", C.c_float),
         ("block_size", C.c_uint32),
+        ("sweep_mode", C.c_uint32),
+        ("pair_list_capacity", C.c_uint32),
     ]
 
 

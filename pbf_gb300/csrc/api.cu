@@ -142,10 +142,12 @@ void apply_tuning(DevConsts& c, const pbf_params& p, const pbf_tuning& t) {
 
 pbf_tuning default_tuning() {
     pbf_tuning t{};
-    t.use_neighbour_lists = 1;
+    t.use_neighbour_lists = 0;
     t.list_capacity = 128;
     t.skin_h = 0.15f;
     t.block_size = 256;
+    t.sweep_mode = PBF_SWEEP_MASKED;
+    t.pair_list_capacity = 64;
     return t;
 }
 
@@ -184,6 +186,20 @@ cudaError_t ensure_lists(pbf_sim* s) {
         if (e != cudaSuccess) return e;
         s->nbr_cap = cap;
     }
+    const uint32_t pcap = s->tuning.pair_list_capacity;
+    if (pcap != s->pair_cap || (pcap > 0 && !s->pair_cnt)) {
+        if (s->pair_idx) cudaFree(s->pair_idx);
+        if (s->pair_cnt) cudaFree(s->pair_cnt);
+        s->pair_idx = nullptr;
+        s->pair_cnt = nullptr;
+        s->pair_cap = 0;
+        if (pcap > 0) {
+            cudaError_t e = dalloc(&s->pair_idx, (size_t)pcap * s->n);
+            if (e == cudaSuccess) e = dalloc(&s->pair_cnt, s->n);
+            if (e != cudaSuccess) return e;
+            s->pair_cap = pcap;
+        }
+    }
     const uint32_t slots = 2 + s->params.num_solver_iterations;
     if (slots > s->guard_slots) {
         if (s->guard) cudaFree(s->guard);
@@ -208,7 +224,7 @@ void free_sim(pbf_sim* s) {
     void* bufs[] = {s->x,  s->v,  s->xstar, s->XP,   s->Pa,     s->Pb,   s->L,
                     s->VS, s->VX, s->OM,    s->Q,    s->keys,   s->skeys, s->perm,
                     s->cstart, s->cend, s->status, s->sort_mem, s->nbr_idx, s->nbr_cnt,
-                    s->guard, s->d_consts, s->sid, s->sid_sorted};
+                    s->guard, s->d_consts, s->sid, s->sid_sorted, s->pair_idx, s->pair_cnt};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (s->h_status) cudaFreeHost(s->h_status);
@@ -282,7 +298,8 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
     if (!s->nbr_cnt || s->guard_slots < 2 + s->params.num_solver_iterations)
         return cudaErrorInvalidValue;  // ensure_lists() runs before any capture
     const unsigned g = grid_for(n);
-    const unsigned sb = s->tuning.block_size ? s->tuning.block_size : (unsigned)kBlock;
+    const SweepCfg sb{s->tuning.block_size ? s->tuning.block_size : (unsigned)kBlock,
+                      s->tuning.sweep_mode == PBF_SWEEP_MASKED};
     const uint32_t iters = s->params.num_solver_iterations;
     cudaStream_t st = s->stream;
     auto mark = [&](uint32_t idx) {
@@ -305,6 +322,7 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
     // 4 solver iterations (calclambda / updatepos).  The first lambda sweep
     // also records the neighbour lists the later sweeps replay.
     const NbrLists nl{s->nbr_idx, s->nbr_cnt, s->guard, s->nbr_cap, n};
+    const PairLists pl{s->pair_idx, s->pair_cnt, s->pair_cap, n};
     cudaError_t ge = cudaMemsetAsync(s->guard, 0, sizeof(uint32_t) * (2 + iters), st);
     if (ge != cudaSuccess) return ge;
     const float4* cur = s->XP;
@@ -315,12 +333,14 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
         float4* aux = rec ? rec->AUX[it] : nullptr;
         const int in_slot = it == 0 ? -1 : (int)it;  // displacement of `cur` from XP
         if (it == 0)
-            launch_lambda_build(sb, st, s->XP, s->skeys, s->cstart, s->cend, Lk, aux, nl, n, cps);
+            launch_lambda_build(sb, st, s->XP, s->skeys, s->cstart, s->cend, Lk, aux, nl, pl, n,
+                                cps);
         else
-            launch_lambda(sb, st, cur, s->XP, s->skeys, s->cstart, s->cend, Lk, aux, nl, in_slot, n,
-                          cps);
+            launch_lambda(sb, st, cur, s->XP, s->skeys, s->cstart, s->cend, Lk, aux, nl, pl, in_slot,
+                          n, cps);
         mark(4 + 2 * it);
-        launch_delta_p(sb, st, Lk, s->XP, s->skeys, s->cstart, s->cend, nxt, nl, in_slot,
+        // delta-p replays the pair lists the lambda sweep just recorded
+        launch_delta_p(sb, st, Lk, s->XP, s->skeys, s->cstart, s->cend, nxt, nl, pl, in_slot,
                        (int)it + 1, n, cps, s->status);
         mark(5 + 2 * it);
         cur = nxt;
@@ -341,11 +361,11 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
     mark(4 + 2 * iters);
     if (vort)
         launch_vorticity_a(sb, st, cur, s->XP, VS, s->skeys, s->cstart, s->cend, s->VX, OM, Q, nl,
-                           fin_slot, n, cps);
+                           pl, fin_slot, n, cps);
     mark(5 + 2 * iters);
     if (vort)
         launch_vorticity_b(sb, st, Q, s->XP, s->VX, OM, s->skeys, s->perm, s->cstart, s->cend, s->v,
-                           rec ? rec->ETA : nullptr, nl, fin_slot, n, cps);
+                           rec ? rec->ETA : nullptr, nl, pl, fin_slot, n, cps);
     mark(6 + 2 * iters);
     return cudaGetLastError();
 }
@@ -554,6 +574,10 @@ pbf_status pbf_set_tuning(pbf_sim* s, const pbf_tuning* t) {
     if (t->block_size != 0 && (t->block_size < 32 || t->block_size > (uint32_t)kBlock ||
                                t->block_size % 32 != 0))
         return fail(s, PBF_ERR_INVALID_ARGUMENT, "block_size must be 0 or a multiple of 32 in [32, 256]");
+    if (t->pair_list_capacity > 4096)
+        return fail(s, PBF_ERR_INVALID_ARGUMENT, "pair_list_capacity must be in [0, 4096]");
+    if (t->sweep_mode != PBF_SWEEP_DIRECT && t->sweep_mode != PBF_SWEEP_MASKED)
+        return fail(s, PBF_ERR_INVALID_ARGUMENT, "sweep_mode must be PBF_SWEEP_DIRECT or PBF_SWEEP_MASKED");
     DeviceGuard dg(s->device);
     PBF_CUDA(s, cudaStreamSynchronize(s->stream));
     s->tuning = *t;
@@ -597,18 +621,20 @@ pbf_status pbf_autotune(pbf_sim* s, uint32_t trial_substeps, pbf_tuning* best) {
     }
     const pbf_tuning original = s->tuning;
     std::vector<pbf_tuning> cand;
-    for (uint32_t blk : {128u, 256u}) {
-        pbf_tuning t = original;
-        t.block_size = blk;
-        t.use_neighbour_lists = 0;
-        cand.push_back(t);
-        for (float skin : {0.05f, 0.1f, 0.2f}) {
-            t.use_neighbour_lists = 1;
-            t.skin_h = skin;
-            if (t.list_capacity == 0) t.list_capacity = 128;
+    for (uint32_t blk : {128u, 256u})
+        for (uint32_t mode : {(uint32_t)PBF_SWEEP_DIRECT, (uint32_t)PBF_SWEEP_MASKED}) {
+            pbf_tuning t = original;
+            t.block_size = blk;
+            t.sweep_mode = mode;
+            t.use_neighbour_lists = 0;
             cand.push_back(t);
+            for (float skin : {0.05f, 0.1f, 0.2f}) {
+                t.use_neighbour_lists = 1;
+                t.skin_h = skin;
+                if (t.list_capacity == 0) t.list_capacity = 128;
+                cand.push_back(t);
+            }
         }
-    }
     float best_ms = 1e30f;
     pbf_tuning best_t = original;
     pbf_status r = PBF_OK;

@@ -59,6 +59,18 @@ struct NbrLists {
     uint32_t n;
 };
 
+// Exact pair lists: the candidates within h of each particle (r2 not above
+// r2cut, NaN included) at one set of positions, in visit order, recorded by
+// the sweep that first reads those positions (lambda, vorticity pass A) and
+// replayed by the next sweep over the same positions (delta-p, vorticity
+// pass B).  SoA [cap][n]; cnt -1 when a list overflowed; cap 0 = off.
+struct PairLists {
+    uint32_t* idx;
+    int32_t* cnt;
+    uint32_t cap;
+    uint32_t n;
+};
+
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }

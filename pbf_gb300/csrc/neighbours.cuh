@@ -56,4 +56,42 @@ __device__ __forceinline__ void visit_full(uint32_t i, uint32_t key, const DevCo
             if ((uint32_t)j != i) f((uint32_t)j);
 }
 
+// The candidates of sorted particle i within h of it (r2 not above r2cut at
+// positions X; a NaN distance counts as within, as in the pair bodies), in
+// visit_full's order, in two loops per chunk of up to 32 consecutive
+// candidates of a run: a scan marks the in-range candidates in a register bit
+// mask, then f runs on the marked ones in ascending order.  With most
+// candidates out of range, a warp's lanes then scan together and evaluate
+// pairs together, instead of all lanes waiting while some evaluate a pair
+// inside the scan.  `scan(j, r2)` sees every candidate (j != i) in order.
+template <class S, class F>
+__device__ __forceinline__ void visit_masked(uint32_t i, uint32_t key, const DevConsts& c,
+                                             const int32_t* __restrict__ cstart,
+                                             const int32_t* __restrict__ cend,
+                                             const float4* __restrict__ X, float3 pi, S&& scan,
+                                             F&& f) {
+    Runs r;
+    runs_of(key, c, cstart, cend, r);
+#pragma unroll 1
+    for (int o = 0; o < 9; ++o)
+        for (int32_t base = r.b[o]; base < r.e[o]; base += 32) {
+            const int32_t m_end = min(r.e[o] - base, 32);
+            uint32_t m = 0;
+            for (int32_t t = 0; t < m_end; ++t) {
+                const uint32_t j = (uint32_t)(base + t);
+                if (j == i) continue;
+                const float4 xj = __ldg(X + j);
+                const float3 d = sub3(pi, make_float3(xj.x, xj.y, xj.z));
+                const float r2 = dot3(d, d);
+                scan(j, r2);
+                if (!(r2 > c.r2cut)) m |= 1u << t;
+            }
+            while (m) {
+                const int t = __ffs(m) - 1;
+                m &= m - 1;
+                f((uint32_t)(base + t));
+            }
+        }
+}
+
 }  // namespace pbf

@@ -51,6 +51,10 @@ struct pbf_sim {
     uint32_t* guard = nullptr;
     uint32_t nbr_cap = 0;       // capacity of nbr_idx in entries per particle
     uint32_t guard_slots = 0;
+    // exact pair lists (PairLists), recorded and replayed within a substep
+    uint32_t* pair_idx = nullptr;
+    int32_t* pair_cnt = nullptr;
+    uint32_t pair_cap = 0;
     uint32_t* h_status = nullptr;
     void* sort_mem = nullptr;
     SortWorkspace sort;

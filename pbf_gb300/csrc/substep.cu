@@ -109,6 +109,32 @@ __device__ __forceinline__ void visit_list(uint32_t i, int32_t cnt, const NbrLis
     for (int32_t k = 0; k < cnt; ++k) f(__ldg(p + (size_t)k * nl.n));
 }
 
+// Writer of particle i's exact pair list (PairLists): appends in visit order,
+// counts past the capacity, and marks an overflowed list with -1.
+struct PairRecorder {
+    const PairLists& pl;
+    uint32_t i;
+    uint32_t k;
+    __device__ __forceinline__ void operator()(uint32_t j) {
+        if (k < pl.cap) pl.idx[(size_t)k * pl.n + i] = j;
+        ++k;
+    }
+    __device__ __forceinline__ void finish() const {
+        if (pl.cap) pl.cnt[i] = k <= pl.cap ? (int32_t)k : -1;
+    }
+};
+
+// Replays particle i's exact pair list when one was recorded and fits.
+template <class F>
+__device__ __forceinline__ bool visit_pairs(uint32_t i, const PairLists& pl, F&& f) {
+    if (!pl.cap) return false;
+    const int32_t cnt = pl.cnt[i];
+    if (cnt < 0) return false;
+    const uint32_t* __restrict__ p = pl.idx + i;
+    for (int32_t k = 0; k < cnt; ++k) f(__ldg(p + (size_t)k * pl.n));
+    return true;
+}
+
 // Guard: may particle i (current position pi, predicted position xi) use
 // its list in a sweep whose positions have moved at most dmax from the
 // predicted ones?  NaN anywhere makes the answer false.
@@ -130,6 +156,18 @@ __device__ __forceinline__ void warp_max_to(uint32_t* slot, float v) {
     if ((threadIdx.x & 31) == 0) atomicMax(slot, b);
 }
 
+// The full-stencil visit of a sweep: direct, or scan-then-evaluate by chunks.
+template <bool MASKED, class F>
+__device__ __forceinline__ void sweep_visit(uint32_t i, uint32_t key, const DevConsts& c,
+                                            const int32_t* __restrict__ cstart,
+                                            const int32_t* __restrict__ cend,
+                                            const float4* __restrict__ X, float3 pi, F&& body) {
+    if constexpr (MASKED)
+        visit_masked(i, key, c, cstart, cend, X, pi, [](uint32_t, float) {}, body);
+    else
+        visit_full(i, key, c, cstart, cend, body);
+}
+
 // ---- pair bodies (shared by both visitors) ---------------------------------------
 
 struct LambdaAcc {
@@ -138,8 +176,8 @@ struct LambdaAcc {
 };
 
 // calclambda.glsl:75-95 for one neighbour at offset d = p_i - p_j, r2 = |d|^2.
+// (call only for r2 not above r2cut: len > h gives Wpoly6 = gradWspiky = 0)
 __device__ __forceinline__ void lambda_pair(const DevConsts& c, float3 d, float r2, LambdaAcc& a) {
-    if (r2 > c.r2cut) return;  // len > h: Wpoly6 = gradWspiky = 0
     const float len = fsqrt(r2);
     a.rho = fadd(a.rho, w_poly6(c, len));  // :80-82
     if (len == 0.0f) return;               // gradWspiky(0) = 0 (:60)
@@ -177,11 +215,12 @@ constexpr int kSweepBlocksPerSM = 8;
 // positions XP: a full stencil scan that also records, in visit order, every
 // candidate within h + skin (the neighbour list of the later sweeps) and the
 // largest coordinate magnitude (for the guard's rounding margin).
-template <class CP>
+template <class CP, bool MASKED>
 __global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
 k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys,
                const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
-               float4* __restrict__ L, float4* __restrict__ aux, NbrLists nl, uint32_t n, CP cp) {
+               float4* __restrict__ L, float4* __restrict__ aux, NbrLists nl, PairLists pw,
+               uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < n;
     float3 pi = make_float3(0.0f, 0.0f, 0.0f);
@@ -189,18 +228,33 @@ k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys
         const auto& c = cp.at(i);
         pi = xyz(XP[i]);
         LambdaAcc a{0.0f, 0.0f, make_float3(0.0f, 0.0f, 0.0f)};
+        PairRecorder rec{pw, i, 0u};
         int32_t cnt = 0;
         const uint32_t cap = c.use_lists ? nl.cap : 0u;
-        visit_full(i, skeys[i], c, cstart, cend, [&](uint32_t j) {
-            const float3 d = sub3(pi, xyz(__ldg(XP + j)));
-            const float r2 = dot3(d, d);
+        auto record = [&](uint32_t j, float r2) {
             if (r2 <= c.r2list) {
                 if ((uint32_t)cnt < cap) nl.idx[(size_t)cnt * n + i] = j;
                 ++cnt;
             }
-            lambda_pair(c, d, r2, a);
-        });
+        };
+        if constexpr (MASKED) {
+            visit_masked(i, skeys[i], c, cstart, cend, XP, pi, record, [&](uint32_t j) {
+                const float3 d = sub3(pi, xyz(__ldg(XP + j)));
+                rec(j);
+                lambda_pair(c, d, dot3(d, d), a);
+            });
+        } else {
+            visit_full(i, skeys[i], c, cstart, cend, [&](uint32_t j) {
+                const float3 d = sub3(pi, xyz(__ldg(XP + j)));
+                const float r2 = dot3(d, d);
+                record(j, r2);
+                if (r2 > c.r2cut) return;
+                rec(j);
+                lambda_pair(c, d, r2, a);
+            });
+        }
         nl.cnt[i] = (uint32_t)cnt <= cap ? cnt : -1;
+        rec.finish();
         L[i] = make_float4(pi.x, pi.y, pi.z, lambda_finish(c, a));
         if (aux) aux[i] = lambda_aux(a);
     }
@@ -210,38 +264,43 @@ k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys
 
 // calclambda.glsl:66-102 at positions P (iterations after the first).
 // dmax_slot: guard slot holding the largest displacement of P from XP.
-template <class CP>
+template <class CP, bool MASKED>
 __global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
 k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
          const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cstart,
          const int32_t* __restrict__ cend, float4* __restrict__ L, float4* __restrict__ aux,
-         NbrLists nl, int dmax_slot, uint32_t n, CP cp) {
+         NbrLists nl, PairLists pw, int dmax_slot, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const auto& c = cp.at(i);
     const float3 pi = xyz(P[i]);
     LambdaAcc a{0.0f, 0.0f, make_float3(0.0f, 0.0f, 0.0f)};
+    PairRecorder rec{pw, i, 0u};
     auto body = [&](uint32_t j) {
         const float3 d = sub3(pi, xyz(__ldg(P + j)));
-        lambda_pair(c, d, dot3(d, d), a);
+        const float r2 = dot3(d, d);
+        if (r2 > c.r2cut) return;
+        rec(j);
+        lambda_pair(c, d, r2, a);
     };
     const int32_t cnt = nl.cnt[i];
     if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot))
         visit_list(i, cnt, nl, body);
     else
-        visit_full(i, skeys[i], c, cstart, cend, body);
+        sweep_visit<MASKED>(i, skeys[i], c, cstart, cend, P, pi, body);
+    rec.finish();
     L[i] = make_float4(pi.x, pi.y, pi.z, lambda_finish(c, a));
     if (aux) aux[i] = lambda_aux(a);
 }
 
 // updatepos.glsl:42-104.  Reads L = (p, lambda), writes clamped positions Pn
 // and the largest displacement of Pn from XP into guard slot `out_slot`.
-template <class CP>
+template <class CP, bool MASKED>
 __global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
 k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
           const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cstart,
-          const int32_t* __restrict__ cend, float4* __restrict__ Pn, NbrLists nl, int dmax_slot,
-          int out_slot, uint32_t n, CP cp, uint32_t* status) {
+          const int32_t* __restrict__ cend, float4* __restrict__ Pn, NbrLists nl, PairLists pr,
+          int dmax_slot, int out_slot, uint32_t n, CP cp, uint32_t* status) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < n;
     float disp = 0.0f;
@@ -267,11 +326,13 @@ k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
             dp = fma3(coef, g, dp);                      // :65
         };
         const float3 xi = xyz(XP[i]);
-        const int32_t cnt = nl.cnt[i];
-        if (list_usable(c, nl, cnt, pi, xi, dmax_slot))
-            visit_list(i, cnt, nl, body);
-        else
-            visit_full(i, skeys[i], c, cstart, cend, body);
+        if (!visit_pairs(i, pr, body)) {
+            const int32_t cnt = nl.cnt[i];
+            if (list_usable(c, nl, cnt, pi, xi, dmax_slot))
+                visit_list(i, cnt, nl, body);
+            else
+                sweep_visit<MASKED>(i, skeys[i], c, cstart, cend, L, pi, body);
+        }
         float3 q = fma3(c.oorho, dp, pi);  // :85
         // clamp (:100) as min(max(q, lo), hi) with explicit selects, so signed
         // zeros and NaN behave like the oracle's std::min/std::max
@@ -311,24 +372,25 @@ k_commit(const float4* __restrict__ P, const uint32_t* __restrict__ perm, float4
 
 // vorticity.glsl:34-60: XSPH velocity and the vorticity vector, Jacobi
 // (every read sees the committed velocities).
-template <class CP>
+template <class CP, bool MASKED>
 __global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
 k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
               const float4* __restrict__ VS, const uint32_t* __restrict__ skeys,
               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
               float4* __restrict__ VX, float4* __restrict__ OM, float4* __restrict__ Q,
-              NbrLists nl, int dmax_slot, uint32_t n, CP cp) {
+              NbrLists nl, PairLists pw, int dmax_slot, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const auto& c = cp.at(i);
     const float3 pi = xyz(P[i]);
     const float3 vi = xyz(VS[i]);
     float3 acc = make_float3(0.0f, 0.0f, 0.0f), w = make_float3(0.0f, 0.0f, 0.0f);
-    auto pos = [&](uint32_t j) { return xyz(__ldg(P + j)); };
+    PairRecorder rec{pw, i, 0u};
     auto body = [&](uint32_t j) {
-        const float3 d = sub3(pi, pos(j));  // :51
+        const float3 d = sub3(pi, xyz(__ldg(P + j)));  // :51
         const float r2 = dot3(d, d);
         if (r2 > c.r2cut) return;
+        rec(j);
         const float len = fsqrt(r2);
         const float3 vij = sub3(xyz(__ldg(VS + j)), vi);  // :50
         acc = fma3(w_poly6(c, len), vij, acc);            // :52-54
@@ -340,7 +402,8 @@ k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
     if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot))
         visit_list(i, cnt, nl, body);
     else
-        visit_full(i, skeys[i], c, cstart, cend, body);
+        sweep_visit<MASKED>(i, skeys[i], c, cstart, cend, P, pi, body);
+    rec.finish();
     const float3 vx = fma3(c.cx, acc, vi);  // :58
     VX[i] = make_float4(vx.x, vx.y, vx.z, 0.0f);
     OM[i] = make_float4(w.x, w.y, w.z, 0.0f);
@@ -349,20 +412,19 @@ k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
 
 // vorticity.glsl:65-85: confinement from the gradient of |vorticity|; writes
 // the final velocity in id order.
-template <class CP>
+template <class CP, bool MASKED>
 __global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
 k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ XP,
               const float4* __restrict__ VX, const float4* __restrict__ OM,
               const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
-              float4* __restrict__ v, float4* __restrict__ eta_out, NbrLists nl, int dmax_slot,
-              uint32_t n, CP cp) {
+              float4* __restrict__ v, float4* __restrict__ eta_out, NbrLists nl, PairLists pr,
+              int dmax_slot, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const auto& c = cp.at(i);
     const float3 pi = xyz(Q[i]);
     float3 eta = make_float3(0.0f, 0.0f, 0.0f);
-    auto pos = [&](uint32_t j) { return xyz(__ldg(Q + j)); };
     auto body = [&](uint32_t j) {
         const float4 Qj = __ldg(Q + j);
         const float3 d = sub3(pi, xyz(Qj));  // :69
@@ -372,11 +434,13 @@ k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ XP,
         if (len == 0.0f) return;
         eta = fma3(Qj.w, scale3(d, grad_scale(c.kg, c.h, len)), eta);  // :72
     };
-    const int32_t cnt = nl.cnt[i];
-    if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot))
-        visit_list(i, cnt, nl, body);
-    else
-        visit_full(i, skeys[i], c, cstart, cend, body);
+    if (!visit_pairs(i, pr, body)) {
+        const int32_t cnt = nl.cnt[i];
+        if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot))
+            visit_list(i, cnt, nl, body);
+        else
+            sweep_visit<MASKED>(i, skeys[i], c, cstart, cend, Q, pi, body);
+    }
     if (eta_out) eta_out[i] = make_float4(eta.x, eta.y, eta.z, 0.0f);
     const float l = fsqrt(dot3(eta, eta));  // :76
     if (l > 0.0f) eta = make_float3(fdiv(eta.x, l), fdiv(eta.y, l), fdiv(eta.z, l));  // :77-78
@@ -467,23 +531,41 @@ void launch_keys_of(unsigned g, cudaStream_t st, const float4* x, float4* xstar,
     k_keys_of<CP><<<g, kBlock, 0, st>>>(x, xstar, keys, n, cp);
 }
 template <class CP>
-void launch_lambda_build(unsigned block, cudaStream_t st, const float4* XP, const uint32_t* skeys,
+void launch_lambda_build(SweepCfg sw, cudaStream_t st, const float4* XP, const uint32_t* skeys,
                          const int32_t* cstart, const int32_t* cend, float4* L, float4* aux,
-                         NbrLists nl, uint32_t n, CP cp) {
-    k_lambda_build<CP><<<grid_for(n, (int)block), block, 0, st>>>(XP, skeys, cstart, cend, L, aux, nl, n, cp);
+                         NbrLists nl, PairLists pw, uint32_t n, CP cp) {
+    const unsigned g = grid_for(n, (int)sw.block);
+    if (sw.masked)
+        k_lambda_build<CP, true><<<g, sw.block, 0, st>>>(XP, skeys, cstart, cend, L, aux, nl, pw,
+                                                                 n, cp);
+    else
+        k_lambda_build<CP, false><<<g, sw.block, 0, st>>>(XP, skeys, cstart, cend, L, aux, nl, pw, n,
+                                                          cp);
 }
 template <class CP>
-void launch_lambda(unsigned block, cudaStream_t st, const float4* P, const float4* XP,
+void launch_lambda(SweepCfg sw, cudaStream_t st, const float4* P, const float4* XP,
                    const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* L,
-                   float4* aux, NbrLists nl, int dmax_slot, uint32_t n, CP cp) {
-    k_lambda<CP><<<grid_for(n, (int)block), block, 0, st>>>(P, XP, skeys, cstart, cend, L, aux, nl, dmax_slot, n, cp);
+                   float4* aux, NbrLists nl, PairLists pw, int dmax_slot, uint32_t n, CP cp) {
+    const unsigned g = grid_for(n, (int)sw.block);
+    if (sw.masked)
+        k_lambda<CP, true><<<g, sw.block, 0, st>>>(P, XP, skeys, cstart, cend, L, aux, nl, pw,
+                                                           dmax_slot, n, cp);
+    else
+        k_lambda<CP, false><<<g, sw.block, 0, st>>>(P, XP, skeys, cstart, cend, L, aux, nl, pw,
+                                                    dmax_slot, n, cp);
 }
 template <class CP>
-void launch_delta_p(unsigned block, cudaStream_t st, const float4* L, const float4* XP,
+void launch_delta_p(SweepCfg sw, cudaStream_t st, const float4* L, const float4* XP,
                     const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* Pn,
-                    NbrLists nl, int dmax_slot, int out_slot, uint32_t n, CP cp, uint32_t* status) {
-    k_delta_p<CP><<<grid_for(n, (int)block), block, 0, st>>>(L, XP, skeys, cstart, cend, Pn, nl, dmax_slot, out_slot, n,
-                                        cp, status);
+                    NbrLists nl, PairLists pr, int dmax_slot, int out_slot, uint32_t n, CP cp,
+                    uint32_t* status) {
+    const unsigned g = grid_for(n, (int)sw.block);
+    if (sw.masked)
+        k_delta_p<CP, true><<<g, sw.block, 0, st>>>(L, XP, skeys, cstart, cend, Pn, nl, pr,
+                                                            dmax_slot, out_slot, n, cp, status);
+    else
+        k_delta_p<CP, false><<<g, sw.block, 0, st>>>(L, XP, skeys, cstart, cend, Pn, nl, pr, dmax_slot,
+                                                     out_slot, n, cp, status);
 }
 template <class CP>
 void launch_commit(unsigned g, cudaStream_t st, const float4* P, const uint32_t* perm, float4* x,
@@ -491,21 +573,32 @@ void launch_commit(unsigned g, cudaStream_t st, const float4* P, const uint32_t*
     k_commit<CP><<<g, kBlock, 0, st>>>(P, perm, x, VS, v_out, n, cp);
 }
 template <class CP>
-void launch_vorticity_a(unsigned block, cudaStream_t st, const float4* P, const float4* XP,
+void launch_vorticity_a(SweepCfg sw, cudaStream_t st, const float4* P, const float4* XP,
                         const float4* VS, const uint32_t* skeys, const int32_t* cstart,
                         const int32_t* cend, float4* VX, float4* OM, float4* Q, NbrLists nl,
-                        int dmax_slot, uint32_t n, CP cp) {
-    k_vorticity_a<CP><<<grid_for(n, (int)block), block, 0, st>>>(P, XP, VS, skeys, cstart, cend, VX, OM, Q, nl,
-                                            dmax_slot, n, cp);
+                        PairLists pw, int dmax_slot, uint32_t n, CP cp) {
+    const unsigned g = grid_for(n, (int)sw.block);
+    if (sw.masked)
+        k_vorticity_a<CP, true><<<g, sw.block, 0, st>>>(P, XP, VS, skeys, cstart, cend, VX,
+                                                                OM, Q, nl, pw, dmax_slot, n, cp);
+    else
+        k_vorticity_a<CP, false><<<g, sw.block, 0, st>>>(P, XP, VS, skeys, cstart, cend, VX, OM, Q,
+                                                         nl, pw, dmax_slot, n, cp);
 }
 template <class CP>
-void launch_vorticity_b(unsigned block, cudaStream_t st, const float4* Q, const float4* XP,
+void launch_vorticity_b(SweepCfg sw, cudaStream_t st, const float4* Q, const float4* XP,
                         const float4* VX, const float4* OM, const uint32_t* skeys,
                         const uint32_t* perm, const int32_t* cstart, const int32_t* cend,
-                        float4* v, float4* eta_out, NbrLists nl, int dmax_slot, uint32_t n,
-                        CP cp) {
-    k_vorticity_b<CP><<<grid_for(n, (int)block), block, 0, st>>>(Q, XP, VX, OM, skeys, perm, cstart, cend, v, eta_out,
-                                            nl, dmax_slot, n, cp);
+                        float4* v, float4* eta_out, NbrLists nl, PairLists pr, int dmax_slot,
+                        uint32_t n, CP cp) {
+    const unsigned g = grid_for(n, (int)sw.block);
+    if (sw.masked)
+        k_vorticity_b<CP, true><<<g, sw.block, 0, st>>>(Q, XP, VX, OM, skeys, perm, cstart,
+                                                                cend, v, eta_out, nl, pr, dmax_slot, n,
+                                                                cp);
+    else
+        k_vorticity_b<CP, false><<<g, sw.block, 0, st>>>(Q, XP, VX, OM, skeys, perm, cstart, cend, v,
+                                                         eta_out, nl, pr, dmax_slot, n, cp);
 }
 template <class CP>
 void launch_diagnostics(unsigned g, cudaStream_t st, const float4* P, const float4* v,
@@ -519,25 +612,26 @@ void launch_diagnostics(unsigned g, cudaStream_t st, const float4* P, const floa
                                      float4*, uint32_t*, uint32_t, CP, uint32_t*);              \
     template void launch_keys_of<CP>(unsigned, cudaStream_t, const float4*, float4*, uint32_t*, \
                                      uint32_t, CP);                                             \
-    template void launch_lambda_build<CP>(unsigned, cudaStream_t, const float4*, const uint32_t*, \
+    template void launch_lambda_build<CP>(SweepCfg, cudaStream_t, const float4*, const uint32_t*, \
                                           const int32_t*, const int32_t*, float4*, float4*,     \
-                                          NbrLists, uint32_t, CP);                              \
-    template void launch_lambda<CP>(unsigned, cudaStream_t, const float4*, const float4*,       \
+                                          NbrLists, PairLists, uint32_t, CP);                   \
+    template void launch_lambda<CP>(SweepCfg, cudaStream_t, const float4*, const float4*,       \
                                     const uint32_t*, const int32_t*, const int32_t*, float4*,   \
-                                    float4*, NbrLists, int, uint32_t, CP);                      \
-    template void launch_delta_p<CP>(unsigned, cudaStream_t, const float4*, const float4*,      \
+                                    float4*, NbrLists, PairLists, int, uint32_t, CP);           \
+    template void launch_delta_p<CP>(SweepCfg, cudaStream_t, const float4*, const float4*,      \
                                      const uint32_t*, const int32_t*, const int32_t*, float4*,  \
-                                     NbrLists, int, int, uint32_t, CP, uint32_t*);              \
+                                     NbrLists, PairLists, int, int, uint32_t, CP, uint32_t*);   \
     template void launch_commit<CP>(unsigned, cudaStream_t, const float4*, const uint32_t*,     \
                                     float4*, float4*, float4*, uint32_t, CP);                   \
-    template void launch_vorticity_a<CP>(unsigned, cudaStream_t, const float4*, const float4*,  \
+    template void launch_vorticity_a<CP>(SweepCfg, cudaStream_t, const float4*, const float4*,  \
                                          const float4*, const uint32_t*, const int32_t*,        \
                                          const int32_t*, float4*, float4*, float4*, NbrLists,   \
-                                         int, uint32_t, CP);                                    \
-    template void launch_vorticity_b<CP>(unsigned, cudaStream_t, const float4*, const float4*,  \
+                                         PairLists, int, uint32_t, CP);                         \
+    template void launch_vorticity_b<CP>(SweepCfg, cudaStream_t, const float4*, const float4*,  \
                                          const float4*, const float4*, const uint32_t*,         \
                                          const uint32_t*, const int32_t*, const int32_t*,       \
-                                         float4*, float4*, NbrLists, int, uint32_t, CP);        \
+                                         float4*, float4*, NbrLists, PairLists, int, uint32_t,  \
+                                         CP);                                                   \
     template void launch_diagnostics<CP>(unsigned, cudaStream_t, const float4*, const float4*,  \
                                          const uint32_t*, const uint32_t*, const int32_t*,      \
                                          const int32_t*, float4*, uint32_t, CP);

@@ -18,6 +18,14 @@ __global__ void k_find_cells(const uint32_t* __restrict__ skeys, const uint32_t*
 // OneScene and ManyScenes in substep.cu).  The neighbour-sweep launchers take
 // their block size (32..256, a multiple of 32); the others take a grid of
 // kBlock-thread blocks.
+// Launch shape of the neighbour sweeps: threads per block, and whether the
+// full-stencil scans mark in-range candidates before evaluating them
+// (visit_masked) or evaluate each where they find it (visit_full).
+struct SweepCfg {
+    unsigned block;
+    bool masked;
+};
+
 template <class CP>
 void launch_predict(unsigned g, cudaStream_t st, const float4* x, const float4* v, float4* xstar,
                     uint32_t* keys, uint32_t n, CP cp, uint32_t* status);
@@ -25,31 +33,32 @@ template <class CP>
 void launch_keys_of(unsigned g, cudaStream_t st, const float4* x, float4* xstar, uint32_t* keys,
                     uint32_t n, CP cp);
 template <class CP>
-void launch_lambda_build(unsigned block, cudaStream_t st, const float4* XP, const uint32_t* skeys,
+void launch_lambda_build(SweepCfg sw, cudaStream_t st, const float4* XP, const uint32_t* skeys,
                          const int32_t* cstart, const int32_t* cend, float4* L, float4* aux,
-                         NbrLists nl, uint32_t n, CP cp);
+                         NbrLists nl, PairLists pw, uint32_t n, CP cp);
 template <class CP>
-void launch_lambda(unsigned block, cudaStream_t st, const float4* P, const float4* XP,
+void launch_lambda(SweepCfg sw, cudaStream_t st, const float4* P, const float4* XP,
                    const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* L,
-                   float4* aux, NbrLists nl, int dmax_slot, uint32_t n, CP cp);
+                   float4* aux, NbrLists nl, PairLists pw, int dmax_slot, uint32_t n, CP cp);
 template <class CP>
-void launch_delta_p(unsigned block, cudaStream_t st, const float4* L, const float4* XP,
+void launch_delta_p(SweepCfg sw, cudaStream_t st, const float4* L, const float4* XP,
                     const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* Pn,
-                    NbrLists nl, int dmax_slot, int out_slot, uint32_t n, CP cp, uint32_t* status);
+                    NbrLists nl, PairLists pr, int dmax_slot, int out_slot, uint32_t n, CP cp,
+                    uint32_t* status);
 template <class CP>
 void launch_commit(unsigned g, cudaStream_t st, const float4* P, const uint32_t* perm, float4* x,
                    float4* VS, float4* v_out, uint32_t n, CP cp);
 template <class CP>
-void launch_vorticity_a(unsigned block, cudaStream_t st, const float4* P, const float4* XP,
+void launch_vorticity_a(SweepCfg sw, cudaStream_t st, const float4* P, const float4* XP,
                         const float4* VS, const uint32_t* skeys, const int32_t* cstart,
                         const int32_t* cend, float4* VX, float4* OM, float4* Q, NbrLists nl,
-                        int dmax_slot, uint32_t n, CP cp);
+                        PairLists pw, int dmax_slot, uint32_t n, CP cp);
 template <class CP>
-void launch_vorticity_b(unsigned block, cudaStream_t st, const float4* Q, const float4* XP,
+void launch_vorticity_b(SweepCfg sw, cudaStream_t st, const float4* Q, const float4* XP,
                         const float4* VX, const float4* OM, const uint32_t* skeys,
                         const uint32_t* perm, const int32_t* cstart, const int32_t* cend,
-                        float4* v, float4* eta_out, NbrLists nl, int dmax_slot, uint32_t n,
-                        CP cp);
+                        float4* v, float4* eta_out, NbrLists nl, PairLists pr, int dmax_slot,
+                        uint32_t n, CP cp);
 template <class CP>
 void launch_diagnostics(unsigned g, cudaStream_t st, const float4* P, const float4* v,
                         const uint32_t* skeys, const uint32_t* perm, const int32_t* cstart,

@@ -226,9 +226,19 @@ def test_set_params_rejects_grid_change(gpu):
                                     dict(use_neighbour_lists=True, list_capacity=8),
                                     dict(use_neighbour_lists=True, skin_h=0.0),
                                     dict(use_neighbour_lists=True, skin_h=0.5, list_capacity=400),
-                                    dict(use_neighbour_lists=True, skin_h=0.02)])
+                                    dict(use_neighbour_lists=True, skin_h=0.02),
+                                    dict(use_neighbour_lists=False, sweep_mode="direct"),
+                                    dict(use_neighbour_lists=False, sweep_mode="masked"),
+                                    dict(use_neighbour_lists=True, sweep_mode="direct", block_size=96),
+                                    dict(use_neighbour_lists=True, skin_h=0.0, sweep_mode="masked"),
+                                    dict(pair_list_capacity=0),
+                                    dict(pair_list_capacity=1, sweep_mode="direct"),
+                                    dict(pair_list_capacity=20, use_neighbour_lists=False),
+                                    dict(pair_list_capacity=4096, use_neighbour_lists=True)])
 def test_tuning_never_changes_results(gpu, oracle_mod, tuning):
-    """Neighbour lists, their capacity and skin are performance knobs only."""
+    """Neighbour lists, their capacity and skin, the sweep mode and the pair
+    lists (capacity 1 and 20 overflow often, falling back to the scan) are
+    performance knobs only."""
     sc = scenes.plain_16k()
     g = pg.SPH(sc.n, tuple(sc.params.grid), sc.params)
     g.set_tuning(**tuning)
@@ -247,7 +257,10 @@ def test_lists_exact_in_a_calm_scene(gpu, oracle_mod):
     sc = scenes.plain_16k()
     p = sc.params.copy()
     p.epsilon = 5.0
-    g = run_gpu(p, sc.x4, sc.v4, 60)
+    g = pg.SPH(sc.n, tuple(p.grid), p)
+    g.set_tuning(use_neighbour_lists=True, skin_h=0.15)
+    g.set_state(sc.x4, sc.v4)
+    g.step(60)
     o = run_oracle(oracle_mod, p, sc.x4, sc.v4, 60)
     x, v = g.get_state()
     ox, ov = o.get_state()
@@ -277,6 +290,8 @@ def test_block_size_and_autotune_never_change_results(gpu, oracle_mod):
     assert_bits(v, ov, "velocities after autotune")
     with pytest.raises(pg.PbfError):
         g.set_tuning(block_size=48)
+    with pytest.raises(pg.PbfError):
+        g.set_tuning(sweep_mode=2)
 
 
 @pytest.mark.parametrize("after", [0, 1, 5, 12, 16])
