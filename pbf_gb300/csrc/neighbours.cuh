@@ -63,35 +63,51 @@ __device__ __forceinline__ void visit_full(uint32_t i, uint32_t key, const DevCo
 // mask, then f runs on the marked ones in ascending order.  With most
 // candidates out of range, a warp's lanes then scan together and evaluate
 // pairs together, instead of all lanes waiting while some evaluate a pair
-// inside the scan.  `scan(j, r2)` sees every candidate (j != i) in order.
-template <class S, class F>
+// inside the scan.  The scan loop only computes r2 and sets a bit; i itself is
+// masked out once per chunk.  With LIST, `list(base, mask)` also receives,
+// per chunk, the candidates base + t (bit t) with r2 <= c.r2list, before f
+// runs on the chunk.
+template <bool LIST, class S, class F>
 __device__ __forceinline__ void visit_masked(uint32_t i, uint32_t key, const DevConsts& c,
                                              const int32_t* __restrict__ cstart,
                                              const int32_t* __restrict__ cend,
-                                             const float4* __restrict__ X, float3 pi, S&& scan,
+                                             const float4* __restrict__ X, float3 pi, S&& list,
                                              F&& f) {
     Runs r;
     runs_of(key, c, cstart, cend, r);
+    const float cut = c.r2cut;
 #pragma unroll 1
-    for (int o = 0; o < 9; ++o)
-        for (int32_t base = r.b[o]; base < r.e[o]; base += 32) {
-            const int32_t m_end = min(r.e[o] - base, 32);
-            uint32_t m = 0;
-            for (int32_t t = 0; t < m_end; ++t) {
-                const uint32_t j = (uint32_t)(base + t);
-                if (j == i) continue;
-                const float4 xj = __ldg(X + j);
+    for (int o = 0; o < 9; ++o) {
+        const int32_t e = r.e[o];
+#pragma unroll 1
+        for (int32_t base = r.b[o]; base < e; base += 32) {
+            const float4* __restrict__ p = X + base;
+            const float4* const pe = p + min(e - base, 32);
+            uint32_t m = 0, l = 0, bit = 1;
+#pragma unroll 1
+            for (; p < pe; ++p) {
+                const float4 xj = __ldg(p);
                 const float3 d = sub3(pi, make_float3(xj.x, xj.y, xj.z));
                 const float r2 = dot3(d, d);
-                scan(j, r2);
-                if (!(r2 > c.r2cut)) m |= 1u << t;
+                if (!(r2 > cut)) m |= bit;
+                if constexpr (LIST) {
+                    if (r2 <= c.r2list) l |= bit;
+                }
+                bit <<= 1;
             }
+            const uint32_t self = i - (uint32_t)base;
+            if (self < 32u) {
+                m &= ~(1u << self);
+                l &= ~(1u << self);
+            }
+            if constexpr (LIST) list(base, l);
             while (m) {
                 const int t = __ffs(m) - 1;
                 m &= m - 1;
                 f((uint32_t)(base + t));
             }
         }
+    }
 }
 
 }  // namespace pbf

@@ -163,7 +163,7 @@ __device__ __forceinline__ void sweep_visit(uint32_t i, uint32_t key, const DevC
                                             const int32_t* __restrict__ cend,
                                             const float4* __restrict__ X, float3 pi, F&& body) {
     if constexpr (MASKED)
-        visit_masked(i, key, c, cstart, cend, X, pi, [](uint32_t, float) {}, body);
+        visit_masked<false>(i, key, c, cstart, cend, X, pi, [](int32_t, uint32_t) {}, body);
     else
         visit_full(i, key, c, cstart, cend, body);
 }
@@ -238,11 +238,27 @@ k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys
             }
         };
         if constexpr (MASKED) {
-            visit_masked(i, skeys[i], c, cstart, cend, XP, pi, record, [&](uint32_t j) {
+            auto pair = [&](uint32_t j) {
                 const float3 d = sub3(pi, xyz(__ldg(XP + j)));
                 rec(j);
                 lambda_pair(c, d, dot3(d, d), a);
-            });
+            };
+            if (cap) {
+                visit_masked<true>(i, skeys[i], c, cstart, cend, XP, pi,
+                                   [&](int32_t base, uint32_t lm) {
+                                       while (lm) {
+                                           const int t = __ffs(lm) - 1;
+                                           lm &= lm - 1;
+                                           if ((uint32_t)cnt < cap)
+                                               nl.idx[(size_t)cnt * n + i] = (uint32_t)(base + t);
+                                           ++cnt;
+                                       }
+                                   },
+                                   pair);
+            } else {
+                visit_masked<false>(i, skeys[i], c, cstart, cend, XP, pi,
+                                    [](int32_t, uint32_t) {}, pair);
+            }
         } else {
             visit_full(i, skeys[i], c, cstart, cend, [&](uint32_t j) {
                 const float3 d = sub3(pi, xyz(__ldg(XP + j)));
