@@ -224,7 +224,8 @@ void free_sim(pbf_sim* s) {
     void* bufs[] = {s->x,  s->v,  s->xstar, s->XP,   s->Pa,     s->Pb,   s->L,
                     s->VS, s->VX, s->OM,    s->Q,    s->keys,   s->skeys, s->perm,
                     s->cstart, s->cend, s->status, s->sort_mem, s->nbr_idx, s->nbr_cnt,
-                    s->guard, s->d_consts, s->sid, s->sid_sorted, s->pair_idx, s->pair_cnt};
+                    s->guard, s->d_consts, s->sid, s->sid_sorted, s->pair_idx, s->pair_cnt,
+                    s->scan_xy, s->scan_z};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (s->h_status) cudaFreeHost(s->h_status);
@@ -316,8 +317,10 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
     if (e != cudaSuccess) return e;
     mark(2);
     // 3 cell ranges (NeighbourCellFinder::FindNeighbourCells)
+    const size_t half = ((size_t)n + 1) / 2;
+    auto scan_set = [&](int k) { return ScanPos{s->scan_xy + k * half, s->scan_z + k * half}; };
     k_find_cells<<<g, kBlock, 0, st>>>(s->skeys, s->perm, s->xstar, s->XP, n, s->ncells, s->cstart,
-                                       s->cend, s->status + 1, s->sid, s->sid_sorted);
+                                       s->cend, s->status + 1, s->sid, s->sid_sorted, scan_set(0));
     mark(3);
     // 4 solver iterations (calclambda / updatepos).  The first lambda sweep
     // also records the neighbour lists the later sweeps replay.
@@ -326,24 +329,28 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
     cudaError_t ge = cudaMemsetAsync(s->guard, 0, sizeof(uint32_t) * (2 + iters), st);
     if (ge != cudaSuccess) return ge;
     const float4* cur = s->XP;
+    int cur_set = 0;  // scan copy of `cur`
     for (uint32_t it = 0; it < iters; ++it) {
         float4* nxt = (it % 2 == 0) ? s->Pa : s->Pb;
+        const int nxt_set = 1 + (int)(it % 2);
         if (rec && it + 1 == iters) nxt = rec->PF;
         float4* Lk = rec ? rec->L[it] : s->L;
         float4* aux = rec ? rec->AUX[it] : nullptr;
         const int in_slot = it == 0 ? -1 : (int)it;  // displacement of `cur` from XP
         if (it == 0)
-            launch_lambda_build(sb, st, s->XP, s->skeys, s->cstart, s->cend, Lk, aux, nl, pl, n,
-                                cps);
+            launch_lambda_build(sb, st, s->XP, s->skeys, s->cstart, s->cend, Lk, aux, nl, pl,
+                                scan_set(0), n, cps);
         else
-            launch_lambda(sb, st, cur, s->XP, s->skeys, s->cstart, s->cend, Lk, aux, nl, pl, in_slot,
-                          n, cps);
+            launch_lambda(sb, st, cur, s->XP, s->skeys, s->cstart, s->cend, Lk, aux, nl, pl,
+                          scan_set(cur_set), in_slot, n, cps);
         mark(4 + 2 * it);
         // delta-p replays the pair lists the lambda sweep just recorded
-        launch_delta_p(sb, st, Lk, s->XP, s->skeys, s->cstart, s->cend, nxt, nl, pl, in_slot,
-                       (int)it + 1, n, cps, s->status);
+        launch_delta_p(sb, st, Lk, s->XP, s->skeys, s->cstart, s->cend, nxt, nl, pl,
+                       scan_set(cur_set), scan_set(nxt_set), in_slot, (int)it + 1, n, cps,
+                       s->status);
         mark(5 + 2 * it);
         cur = nxt;
+        cur_set = nxt_set;
     }
     if (rec && iters == 0) {
         cudaError_t ce = cudaMemcpyAsync(rec->PF, s->XP, sizeof(float4) * n,
@@ -361,11 +368,11 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
     mark(4 + 2 * iters);
     if (vort)
         launch_vorticity_a(sb, st, cur, s->XP, VS, s->skeys, s->cstart, s->cend, s->VX, OM, Q, nl,
-                           pl, fin_slot, n, cps);
+                           pl, scan_set(cur_set), fin_slot, n, cps);
     mark(5 + 2 * iters);
     if (vort)
         launch_vorticity_b(sb, st, Q, s->XP, s->VX, OM, s->skeys, s->perm, s->cstart, s->cend, s->v,
-                           rec ? rec->ETA : nullptr, nl, pl, fin_slot, n, cps);
+                           rec ? rec->ETA : nullptr, nl, pl, scan_set(cur_set), fin_slot, n, cps);
     mark(6 + 2 * iters);
     return cudaGetLastError();
 }
@@ -464,6 +471,7 @@ pbf_status pbf_create_batch(const pbf_params* scene_params, const uint32_t* scen
     ALLOC(x, n) ALLOC(v, n) ALLOC(xstar, n) ALLOC(XP, n) ALLOC(Pa, n) ALLOC(Pb, n) ALLOC(L, n)
     ALLOC(VS, n) ALLOC(VX, n) ALLOC(OM, n) ALLOC(Q, n) ALLOC(keys, n) ALLOC(skeys, n)
     ALLOC(perm, n) ALLOC(cstart, s->ncells) ALLOC(cend, s->ncells) ALLOC(status, 2)
+    ALLOC(scan_xy, 3 * (((size_t)n + 1) / 2)) ALLOC(scan_z, 3 * (((size_t)n + 1) / 2))
     if (num_scenes > 1) {
         ALLOC(d_consts, num_scenes) ALLOC(sid, n) ALLOC(sid_sorted, n)
     }
@@ -855,7 +863,8 @@ pbf_status pbf_compute_diagnostics(pbf_sim* s, pbf_diagnostics* out) {
     cudaError_t e = sort_pairs(s->sort, s->keys, s->skeys, s->perm, n, s->numbits, s->status, st);
     if (e != cudaSuccess) return cuda_fail(s, e, "diagnostics sort");
     k_find_cells<<<g, kBlock, 0, st>>>(s->skeys, s->perm, s->xstar, s->XP, n, s->ncells, s->cstart,
-                                       s->cend, s->status + 1, s->sid, s->sid_sorted);
+                                       s->cend, s->status + 1, s->sid, s->sid_sorted,
+                                       ScanPos{nullptr, nullptr});
     if (s->nscenes == 1)
         launch_diagnostics(g, st, s->XP, s->v, s->skeys, s->perm, s->cstart, s->cend,
                                             s->VX, n, OneScene{s->dc});
@@ -951,7 +960,8 @@ pbf_status pbf_find_cells(const uint32_t* sorted_keys, uint32_t n, uint32_t num_
     if (e == cudaSuccess) e = cudaMemsetAsync(end, 0xFF, sizeof(int32_t) * (size_t)num_cells, st);
     if (e == cudaSuccess && n > 0) {
         k_find_cells<<<grid_for(n), kBlock, 0, st>>>(sorted_keys, nullptr, nullptr, nullptr, n,
-                                                     num_cells, start, end, bad, nullptr, nullptr);
+                                                     num_cells, start, end, bad, nullptr, nullptr,
+                                                     ScanPos{nullptr, nullptr});
         e = cudaGetLastError();
     }
     uint32_t hbad = 0;

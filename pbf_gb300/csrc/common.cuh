@@ -71,6 +71,23 @@ struct PairLists {
     uint32_t n;
 };
 
+// Scan copy of a sorted position array, read by the masked stencil scans two
+// candidates at a time with packed (float2) arithmetic: x and y of the
+// particle pair (2q, 2q+1) interleaved in xy[q] = (x0, x1, y0, y1), z as a
+// plain array read as the float2 z[q] = (z0, z1).  (n + 1) / 2 entries each.
+struct ScanPos {
+    float4* xy;
+    float2* z;
+};
+
+__device__ __forceinline__ void scanpos_store(const ScanPos& sp, uint32_t i, float x, float y,
+                                              float z) {
+    float* xy = reinterpret_cast<float*>(sp.xy) + 4 * (size_t)(i >> 1) + (i & 1u);
+    xy[0] = x;
+    xy[2] = y;
+    reinterpret_cast<float*>(sp.z)[i] = z;
+}
+
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }

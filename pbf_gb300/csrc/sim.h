@@ -55,6 +55,10 @@ struct pbf_sim {
     uint32_t* pair_idx = nullptr;
     int32_t* pair_cnt = nullptr;
     uint32_t pair_cap = 0;
+    // scan copies (ScanPos) of the predicted positions (set 0) and of the
+    // solver iterates (sets 1 and 2, alternating), (n + 1) / 2 pairs per set
+    float4* scan_xy = nullptr;
+    float2* scan_z = nullptr;
     uint32_t* h_status = nullptr;
     void* sort_mem = nullptr;
     SortWorkspace sort;

@@ -76,11 +76,15 @@ __global__ void __launch_bounds__(kBlock)
 k_find_cells(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
              const float4* __restrict__ xstar, float4* __restrict__ P0, uint32_t n, uint32_t ncells,
              int32_t* __restrict__ cstart, int32_t* __restrict__ cend, uint32_t* bad,
-             const uint32_t* __restrict__ sid, uint32_t* __restrict__ sid_sorted) {
+             const uint32_t* __restrict__ sid, uint32_t* __restrict__ sid_sorted, ScanPos sx) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t k = skeys[i];
-    if (P0) P0[i] = __ldg(xstar + perm[i]);
+    if (P0) {
+        const float4 p = __ldg(xstar + perm[i]);
+        P0[i] = p;
+        if (sx.xy) scanpos_store(sx, i, p.x, p.y, p.z);
+    }
     if (sid_sorted) sid_sorted[i] = __ldg(sid + perm[i]);
     if (k >= ncells) {
         atomicOr(bad, 1u);
@@ -160,8 +164,8 @@ __device__ __forceinline__ void warp_max_to(uint32_t* slot, float v) {
 template <bool MASKED, class F>
 __device__ __forceinline__ void sweep_visit(uint32_t i, uint32_t key, const DevConsts& c,
                                             const int32_t* __restrict__ cstart,
-                                            const int32_t* __restrict__ cend,
-                                            const float4* __restrict__ X, float3 pi, F&& body) {
+                                            const int32_t* __restrict__ cend, const ScanPos& X,
+                                            float3 pi, F&& body) {
     if constexpr (MASKED)
         visit_masked<false>(i, key, c, cstart, cend, X, pi, [](int32_t, uint32_t) {}, body);
     else
@@ -220,7 +224,7 @@ __global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
 k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys,
                const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
                float4* __restrict__ L, float4* __restrict__ aux, NbrLists nl, PairLists pw,
-               uint32_t n, CP cp) {
+               ScanPos sx, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < n;
     float3 pi = make_float3(0.0f, 0.0f, 0.0f);
@@ -244,7 +248,7 @@ k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys
                 lambda_pair(c, d, dot3(d, d), a);
             };
             if (cap) {
-                visit_masked<true>(i, skeys[i], c, cstart, cend, XP, pi,
+                visit_masked<true>(i, skeys[i], c, cstart, cend, sx, pi,
                                    [&](int32_t base, uint32_t lm) {
                                        while (lm) {
                                            const int t = __ffs(lm) - 1;
@@ -256,7 +260,7 @@ k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys
                                    },
                                    pair);
             } else {
-                visit_masked<false>(i, skeys[i], c, cstart, cend, XP, pi,
+                visit_masked<false>(i, skeys[i], c, cstart, cend, sx, pi,
                                     [](int32_t, uint32_t) {}, pair);
             }
         } else {
@@ -285,7 +289,7 @@ __global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
 k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
          const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cstart,
          const int32_t* __restrict__ cend, float4* __restrict__ L, float4* __restrict__ aux,
-         NbrLists nl, PairLists pw, int dmax_slot, uint32_t n, CP cp) {
+         NbrLists nl, PairLists pw, ScanPos sx, int dmax_slot, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const auto& c = cp.at(i);
@@ -303,7 +307,7 @@ k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
     if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot))
         visit_list(i, cnt, nl, body);
     else
-        sweep_visit<MASKED>(i, skeys[i], c, cstart, cend, P, pi, body);
+        sweep_visit<MASKED>(i, skeys[i], c, cstart, cend, sx, pi, body);
     rec.finish();
     L[i] = make_float4(pi.x, pi.y, pi.z, lambda_finish(c, a));
     if (aux) aux[i] = lambda_aux(a);
@@ -316,7 +320,8 @@ __global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
 k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
           const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cstart,
           const int32_t* __restrict__ cend, float4* __restrict__ Pn, NbrLists nl, PairLists pr,
-          int dmax_slot, int out_slot, uint32_t n, CP cp, uint32_t* status) {
+          ScanPos sx, ScanPos sx_out, int dmax_slot, int out_slot, uint32_t n, CP cp,
+          uint32_t* status) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < n;
     float disp = 0.0f;
@@ -347,7 +352,7 @@ k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
             if (list_usable(c, nl, cnt, pi, xi, dmax_slot))
                 visit_list(i, cnt, nl, body);
             else
-                sweep_visit<MASKED>(i, skeys[i], c, cstart, cend, L, pi, body);
+                sweep_visit<MASKED>(i, skeys[i], c, cstart, cend, sx, pi, body);
         }
         float3 q = fma3(c.oorho, dp, pi);  // :85
         // clamp (:100) as min(max(q, lo), hi) with explicit selects, so signed
@@ -360,6 +365,7 @@ k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
         q.z = (c.hi[2] < q.z) ? c.hi[2] : q.z;
         if (!finite3(q)) atomicOr(status, kDevNonFinite);
         Pn[i] = make_float4(q.x, q.y, q.z, 0.0f);
+        if (sx_out.xy) scanpos_store(sx_out, i, q.x, q.y, q.z);
         const float3 dd = make_float3(q.x - xi.x, q.y - xi.y, q.z - xi.z);
         disp = sqrtf(dd.x * dd.x + dd.y * dd.y + dd.z * dd.z);
     }
@@ -394,7 +400,7 @@ k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
               const float4* __restrict__ VS, const uint32_t* __restrict__ skeys,
               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
               float4* __restrict__ VX, float4* __restrict__ OM, float4* __restrict__ Q,
-              NbrLists nl, PairLists pw, int dmax_slot, uint32_t n, CP cp) {
+              NbrLists nl, PairLists pw, ScanPos sx, int dmax_slot, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const auto& c = cp.at(i);
@@ -418,7 +424,7 @@ k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
     if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot))
         visit_list(i, cnt, nl, body);
     else
-        sweep_visit<MASKED>(i, skeys[i], c, cstart, cend, P, pi, body);
+        sweep_visit<MASKED>(i, skeys[i], c, cstart, cend, sx, pi, body);
     rec.finish();
     const float3 vx = fma3(c.cx, acc, vi);  // :58
     VX[i] = make_float4(vx.x, vx.y, vx.z, 0.0f);
@@ -435,7 +441,7 @@ k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ XP,
               const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
               float4* __restrict__ v, float4* __restrict__ eta_out, NbrLists nl, PairLists pr,
-              int dmax_slot, uint32_t n, CP cp) {
+              ScanPos sx, int dmax_slot, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const auto& c = cp.at(i);
@@ -455,7 +461,7 @@ k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ XP,
         if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot))
             visit_list(i, cnt, nl, body);
         else
-            sweep_visit<MASKED>(i, skeys[i], c, cstart, cend, Q, pi, body);
+            sweep_visit<MASKED>(i, skeys[i], c, cstart, cend, sx, pi, body);
     }
     if (eta_out) eta_out[i] = make_float4(eta.x, eta.y, eta.z, 0.0f);
     const float l = fsqrt(dot3(eta, eta));  // :76
@@ -549,38 +555,39 @@ void launch_keys_of(unsigned g, cudaStream_t st, const float4* x, float4* xstar,
 template <class CP>
 void launch_lambda_build(SweepCfg sw, cudaStream_t st, const float4* XP, const uint32_t* skeys,
                          const int32_t* cstart, const int32_t* cend, float4* L, float4* aux,
-                         NbrLists nl, PairLists pw, uint32_t n, CP cp) {
+                         NbrLists nl, PairLists pw, ScanPos sx, uint32_t n, CP cp) {
     const unsigned g = grid_for(n, (int)sw.block);
     if (sw.masked)
-        k_lambda_build<CP, true><<<g, sw.block, 0, st>>>(XP, skeys, cstart, cend, L, aux, nl, pw,
+        k_lambda_build<CP, true><<<g, sw.block, 0, st>>>(XP, skeys, cstart, cend, L, aux, nl, pw, sx,
                                                                  n, cp);
     else
-        k_lambda_build<CP, false><<<g, sw.block, 0, st>>>(XP, skeys, cstart, cend, L, aux, nl, pw, n,
+        k_lambda_build<CP, false><<<g, sw.block, 0, st>>>(XP, skeys, cstart, cend, L, aux, nl, pw, sx, n,
                                                           cp);
 }
 template <class CP>
 void launch_lambda(SweepCfg sw, cudaStream_t st, const float4* P, const float4* XP,
                    const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* L,
-                   float4* aux, NbrLists nl, PairLists pw, int dmax_slot, uint32_t n, CP cp) {
+                   float4* aux, NbrLists nl, PairLists pw, ScanPos sx, int dmax_slot, uint32_t n,
+                   CP cp) {
     const unsigned g = grid_for(n, (int)sw.block);
     if (sw.masked)
-        k_lambda<CP, true><<<g, sw.block, 0, st>>>(P, XP, skeys, cstart, cend, L, aux, nl, pw,
+        k_lambda<CP, true><<<g, sw.block, 0, st>>>(P, XP, skeys, cstart, cend, L, aux, nl, pw, sx,
                                                            dmax_slot, n, cp);
     else
-        k_lambda<CP, false><<<g, sw.block, 0, st>>>(P, XP, skeys, cstart, cend, L, aux, nl, pw,
+        k_lambda<CP, false><<<g, sw.block, 0, st>>>(P, XP, skeys, cstart, cend, L, aux, nl, pw, sx,
                                                     dmax_slot, n, cp);
 }
 template <class CP>
 void launch_delta_p(SweepCfg sw, cudaStream_t st, const float4* L, const float4* XP,
                     const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* Pn,
-                    NbrLists nl, PairLists pr, int dmax_slot, int out_slot, uint32_t n, CP cp,
-                    uint32_t* status) {
+                    NbrLists nl, PairLists pr, ScanPos sx, ScanPos sx_out, int dmax_slot,
+                    int out_slot, uint32_t n, CP cp, uint32_t* status) {
     const unsigned g = grid_for(n, (int)sw.block);
     if (sw.masked)
-        k_delta_p<CP, true><<<g, sw.block, 0, st>>>(L, XP, skeys, cstart, cend, Pn, nl, pr,
+        k_delta_p<CP, true><<<g, sw.block, 0, st>>>(L, XP, skeys, cstart, cend, Pn, nl, pr, sx, sx_out,
                                                             dmax_slot, out_slot, n, cp, status);
     else
-        k_delta_p<CP, false><<<g, sw.block, 0, st>>>(L, XP, skeys, cstart, cend, Pn, nl, pr, dmax_slot,
+        k_delta_p<CP, false><<<g, sw.block, 0, st>>>(L, XP, skeys, cstart, cend, Pn, nl, pr, sx, sx_out, dmax_slot,
                                                      out_slot, n, cp, status);
 }
 template <class CP>
@@ -592,29 +599,29 @@ template <class CP>
 void launch_vorticity_a(SweepCfg sw, cudaStream_t st, const float4* P, const float4* XP,
                         const float4* VS, const uint32_t* skeys, const int32_t* cstart,
                         const int32_t* cend, float4* VX, float4* OM, float4* Q, NbrLists nl,
-                        PairLists pw, int dmax_slot, uint32_t n, CP cp) {
+                        PairLists pw, ScanPos sx, int dmax_slot, uint32_t n, CP cp) {
     const unsigned g = grid_for(n, (int)sw.block);
     if (sw.masked)
         k_vorticity_a<CP, true><<<g, sw.block, 0, st>>>(P, XP, VS, skeys, cstart, cend, VX,
-                                                                OM, Q, nl, pw, dmax_slot, n, cp);
+                                                                OM, Q, nl, pw, sx, dmax_slot, n, cp);
     else
         k_vorticity_a<CP, false><<<g, sw.block, 0, st>>>(P, XP, VS, skeys, cstart, cend, VX, OM, Q,
-                                                         nl, pw, dmax_slot, n, cp);
+                                                         nl, pw, sx, dmax_slot, n, cp);
 }
 template <class CP>
 void launch_vorticity_b(SweepCfg sw, cudaStream_t st, const float4* Q, const float4* XP,
                         const float4* VX, const float4* OM, const uint32_t* skeys,
                         const uint32_t* perm, const int32_t* cstart, const int32_t* cend,
-                        float4* v, float4* eta_out, NbrLists nl, PairLists pr, int dmax_slot,
-                        uint32_t n, CP cp) {
+                        float4* v, float4* eta_out, NbrLists nl, PairLists pr, ScanPos sx,
+                        int dmax_slot, uint32_t n, CP cp) {
     const unsigned g = grid_for(n, (int)sw.block);
     if (sw.masked)
         k_vorticity_b<CP, true><<<g, sw.block, 0, st>>>(Q, XP, VX, OM, skeys, perm, cstart,
-                                                                cend, v, eta_out, nl, pr, dmax_slot, n,
+                                                                cend, v, eta_out, nl, pr, sx, dmax_slot, n,
                                                                 cp);
     else
         k_vorticity_b<CP, false><<<g, sw.block, 0, st>>>(Q, XP, VX, OM, skeys, perm, cstart, cend, v,
-                                                         eta_out, nl, pr, dmax_slot, n, cp);
+                                                         eta_out, nl, pr, sx, dmax_slot, n, cp);
 }
 template <class CP>
 void launch_diagnostics(unsigned g, cudaStream_t st, const float4* P, const float4* v,
@@ -630,24 +637,25 @@ void launch_diagnostics(unsigned g, cudaStream_t st, const float4* P, const floa
                                      uint32_t, CP);                                             \
     template void launch_lambda_build<CP>(SweepCfg, cudaStream_t, const float4*, const uint32_t*, \
                                           const int32_t*, const int32_t*, float4*, float4*,     \
-                                          NbrLists, PairLists, uint32_t, CP);                   \
+                                          NbrLists, PairLists, ScanPos, uint32_t, CP);          \
     template void launch_lambda<CP>(SweepCfg, cudaStream_t, const float4*, const float4*,       \
                                     const uint32_t*, const int32_t*, const int32_t*, float4*,   \
-                                    float4*, NbrLists, PairLists, int, uint32_t, CP);           \
+                                    float4*, NbrLists, PairLists, ScanPos, int, uint32_t, CP);  \
     template void launch_delta_p<CP>(SweepCfg, cudaStream_t, const float4*, const float4*,      \
                                      const uint32_t*, const int32_t*, const int32_t*, float4*,  \
-                                     NbrLists, PairLists, int, int, uint32_t, CP, uint32_t*);   \
+                                     NbrLists, PairLists, ScanPos, ScanPos, int, int, uint32_t, \
+                                     CP, uint32_t*);                                            \
     template void launch_commit<CP>(unsigned, cudaStream_t, const float4*, const uint32_t*,     \
                                     float4*, float4*, float4*, uint32_t, CP);                   \
     template void launch_vorticity_a<CP>(SweepCfg, cudaStream_t, const float4*, const float4*,  \
                                          const float4*, const uint32_t*, const int32_t*,        \
                                          const int32_t*, float4*, float4*, float4*, NbrLists,   \
-                                         PairLists, int, uint32_t, CP);                         \
+                                         PairLists, ScanPos, int, uint32_t, CP);                \
     template void launch_vorticity_b<CP>(SweepCfg, cudaStream_t, const float4*, const float4*,  \
                                          const float4*, const float4*, const uint32_t*,         \
                                          const uint32_t*, const int32_t*, const int32_t*,       \
-                                         float4*, float4*, NbrLists, PairLists, int, uint32_t,  \
-                                         CP);                                                   \
+                                         float4*, float4*, NbrLists, PairLists, ScanPos, int,   \
+                                         uint32_t, CP);                                         \
     template void launch_diagnostics<CP>(unsigned, cudaStream_t, const float4*, const float4*,  \
                                          const uint32_t*, const uint32_t*, const int32_t*,      \
                                          const int32_t*, float4*, uint32_t, CP);

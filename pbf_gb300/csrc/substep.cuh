@@ -12,7 +12,8 @@ __global__ void k_find_cells(const uint32_t* __restrict__ skeys, const uint32_t*
                              const float4* __restrict__ xstar, float4* __restrict__ P0, uint32_t n,
                              uint32_t ncells, int32_t* __restrict__ cstart,
                              int32_t* __restrict__ cend, uint32_t* bad,
-                             const uint32_t* __restrict__ sid, uint32_t* __restrict__ sid_sorted);
+                             const uint32_t* __restrict__ sid, uint32_t* __restrict__ sid_sorted,
+                             ScanPos sx);
 
 // Host launchers of the templated stage kernels (explicitly instantiated for
 // OneScene and ManyScenes in substep.cu).  The neighbour-sweep launchers take
@@ -35,16 +36,17 @@ void launch_keys_of(unsigned g, cudaStream_t st, const float4* x, float4* xstar,
 template <class CP>
 void launch_lambda_build(SweepCfg sw, cudaStream_t st, const float4* XP, const uint32_t* skeys,
                          const int32_t* cstart, const int32_t* cend, float4* L, float4* aux,
-                         NbrLists nl, PairLists pw, uint32_t n, CP cp);
+                         NbrLists nl, PairLists pw, ScanPos sx, uint32_t n, CP cp);
 template <class CP>
 void launch_lambda(SweepCfg sw, cudaStream_t st, const float4* P, const float4* XP,
                    const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* L,
-                   float4* aux, NbrLists nl, PairLists pw, int dmax_slot, uint32_t n, CP cp);
+                   float4* aux, NbrLists nl, PairLists pw, ScanPos sx, int dmax_slot, uint32_t n,
+                   CP cp);
 template <class CP>
 void launch_delta_p(SweepCfg sw, cudaStream_t st, const float4* L, const float4* XP,
                     const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* Pn,
-                    NbrLists nl, PairLists pr, int dmax_slot, int out_slot, uint32_t n, CP cp,
-                    uint32_t* status);
+                    NbrLists nl, PairLists pr, ScanPos sx, ScanPos sx_out, int dmax_slot,
+                    int out_slot, uint32_t n, CP cp, uint32_t* status);
 template <class CP>
 void launch_commit(unsigned g, cudaStream_t st, const float4* P, const uint32_t* perm, float4* x,
                    float4* VS, float4* v_out, uint32_t n, CP cp);
@@ -52,13 +54,13 @@ template <class CP>
 void launch_vorticity_a(SweepCfg sw, cudaStream_t st, const float4* P, const float4* XP,
                         const float4* VS, const uint32_t* skeys, const int32_t* cstart,
                         const int32_t* cend, float4* VX, float4* OM, float4* Q, NbrLists nl,
-                        PairLists pw, int dmax_slot, uint32_t n, CP cp);
+                        PairLists pw, ScanPos sx, int dmax_slot, uint32_t n, CP cp);
 template <class CP>
 void launch_vorticity_b(SweepCfg sw, cudaStream_t st, const float4* Q, const float4* XP,
                         const float4* VX, const float4* OM, const uint32_t* skeys,
                         const uint32_t* perm, const int32_t* cstart, const int32_t* cend,
-                        float4* v, float4* eta_out, NbrLists nl, PairLists pr, int dmax_slot,
-                        uint32_t n, CP cp);
+                        float4* v, float4* eta_out, NbrLists nl, PairLists pr, ScanPos sx,
+                        int dmax_slot, uint32_t n, CP cp);
 template <class CP>
 void launch_diagnostics(unsigned g, cudaStream_t st, const float4* P, const float4* v,
                         const uint32_t* skeys, const uint32_t* perm, const int32_t* cstart,
