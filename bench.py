@@ -64,6 +64,7 @@ def parse():
     ap.add_argument("--no-stable", action="store_true", help="skip the epsilon = 5 full run")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-scene comparison")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the backward/forward ratio")
+    ap.add_argument("--no-splat", action="store_true", help="skip the depth/thickness splatting leg")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--recovery", action="store_true",
                     help="also run the 64-scene parameter recovery (about a minute)")
@@ -206,6 +207,46 @@ def batched_vs_plain(stream, num_scenes: int = 256, substeps: int = 100):
             "plain_scenes_per_s": num_scenes / (tp * 1e-3), "speedup": tp / tb,
             "batched_particle_iters_per_s": n * it * substeps / (tb * 1e-3),
             "bit_identical_sampled_scenes": bool(same)}
+
+
+def splat_leg(stream, reps: int = 20):
+    """SurfaceReconstruction's particle passes (pbf_splat) on the reference's
+    own scene (65,536 particles, after 20 substeps) and camera, at the
+    reference's framebuffer sizes: depth 1280 x 720, thickness 512 x 512.
+    CUDA events around `reps` calls each (each call clears its image and
+    synchronises)."""
+    import torch
+    import pbf_gb300 as pg
+    from pbf_gb300 import scenes, splat
+    s = scenes.reference_two_blocks(seed=0)
+    sim = pg.SPH(s.n, tuple(s.params.grid), s.params)
+    sim.set_stream(stream.cuda_stream)
+    sim.set_state(s.x4, s.v4)
+    sim.step(20)
+    sim.synchronize()
+    view = splat.reference_view(1280, 720)
+    res = {"particles": s.n, "reps": reps}
+    for name, p, (w, h) in (("depth", splat.DEPTH, (1280, 720)),
+                            ("thickness", splat.THICKNESS, (512, 512))):
+        out = torch.empty((h, w), dtype=torch.float32, device="cuda")
+        for _ in range(3):
+            splat.splat_device(p, sim.GetPositionBuffer(), s.n, view, w, h, out.data_ptr(),
+                               stream.cuda_stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            splat.splat_device(p, sim.GetPositionBuffer(), s.n, view, w, h, out.data_ptr(),
+                               stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        res[f"{name}_ms"] = ms
+        res[f"{name}_size"] = [w, h]
+        res[f"{name}_covered_pixels"] = int(((out < 1) if p == splat.DEPTH else (out > 0)).sum().item())
+    res["particles_per_s_depth"] = s.n / (res["depth_ms"] * 1e-3)
+    res["note"] = "each call includes its image clear and a stream synchronisation"
+    sim.close()
+    return res
 
 
 def adjoint_ratio(stream, substeps: int = 64, every: int = 8):
@@ -538,6 +579,9 @@ def main():
     adjoint = None
     if not args.no_adjoint:
         adjoint = adjoint_ratio(stream)
+    splats = None
+    if not args.no_splat:
+        splats = splat_leg(stream)
 
     recov = None
     if args.recovery:
@@ -580,6 +624,7 @@ def main():
             "stable_500": stable,
             "batched_256": batched,
             "adjoint_32k": adjoint,
+            "splat_reference_scene": splats,
             "recovery_64": recov,
             "clocks": clk,
             "cpu_baseline": cpu,

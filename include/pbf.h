@@ -336,6 +336,32 @@ pbf_status pbf_release_record(pbf_sim* sim);
  * substep's sort.  Synchronising. */
 pbf_status pbf_highlight_neighbours(pbf_sim* sim, uint32_t* flags, int where);
 
+/* ---- headless splatting ---------------------------------------------------------- */
+
+/* The camera of SurfaceReconstruction's particle passes: the two matrices of
+ * the reference's TransformationBlock (shaders/particledepth/vertex.glsl:29-32),
+ * column-major as GL and glm store them. */
+typedef struct pbf_view {
+    float viewmat[16];
+    float projmat[16];
+} pbf_view;
+
+enum { PBF_SPLAT_DEPTH = 0, PBF_SPLAT_THICKNESS = 1 };
+
+/* SurfaceReconstruction::Render's particle passes (src/SurfaceReconstruction.cpp:
+ * 176-231) into a device buffer out[height][width] (row 0 at the bottom, as GL
+ * window coordinates), without a GL context:
+ *   PBF_SPLAT_DEPTH      shaders/particledepth: per pixel the smallest sphere
+ *                        depth clip z / clip w, clamped to [0, 1], of the
+ *                        particle sprites covering it; 1 where none does;
+ *   PBF_SPLAT_THICKNESS  shaders/thickness with noise off: per pixel the
+ *                        number of sprites covering it (as float).
+ * positions: float4[n] on the device (xyz used, the layout of the position
+ * buffer).  The reference renders depth at 1280 x 720 and thickness at
+ * 512 x 512 with the same matrices.  Runs on `stream` and synchronises. */
+pbf_status pbf_splat(int pass, const float* positions, uint32_t n, const pbf_view* view,
+                     uint32_t width, uint32_t height, float* out, void* stream);
+
 /* Binary snapshot of the state (no reference counterpart: the reference only
  * resets to its initial blocks, src/Simulation.cpp:303-305): "PBFSTATE",
  * u32 version 1, u32 particle count, u32 scene count, u32 0, then x and v as

@@ -24,7 +24,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libpbf_oracle.so")
-SRC = [os.path.join(HERE, "pbf_oracle.cpp"), os.path.join(HERE, "pbf_oracle.hpp")]
+SRC = [os.path.join(HERE, "pbf_oracle.cpp"), os.path.join(HERE, "pbf_oracle.hpp"),
+       os.path.join(HERE, "pbf_splat_oracle.cpp")]
 
 CXXFLAGS = ["-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"]
 
@@ -36,7 +37,7 @@ def build(force: bool = False) -> str:
             os.path.getmtime(LIB) >= os.path.getmtime(s) for s in SRC):
         return LIB
     tmp = LIB + ".tmp"
-    cmd = [os.environ.get("CXX", "g++")] + CXXFLAGS + ["-o", tmp, SRC[0]]
+    cmd = [os.environ.get("CXX", "g++")] + CXXFLAGS + ["-o", tmp, SRC[0], SRC[2]]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + " ".join(cmd) + "\n" + r.stderr)
@@ -70,6 +71,7 @@ def load() -> C.CDLL:
         lib.pbfo_diagnostics.argtypes = [P, P]
         lib.pbfo_radix_sort.argtypes = [P, C.c_uint32, C.c_uint32, P, P]
         lib.pbfo_highlight.argtypes = [P, P]
+        lib.pbfo_splat.argtypes = [C.c_int, P, C.c_uint32, P, P, C.c_uint32, C.c_uint32, P]
         lib.pbfo_max_threads.restype = C.c_int
         lib.pbfo_sample_substep.restype = C.c_double
         lib.pbfo_sample_substep.argtypes = [P, C.c_uint32, C.c_uint32, P, P]
@@ -186,6 +188,20 @@ def radix_sort(keys, numbits: int):
     return ko, po
 
 
+def splat(pass_: int, x4, viewmat, projmat, width: int, height: int):
+    """SurfaceReconstruction's particle passes on the CPU (pbf_splat_oracle.cpp):
+    pass 0 depth, 1 thickness; matrices column-major (16 floats).  Returns
+    float32 [height, width], row 0 at the bottom."""
+    x = np.ascontiguousarray(x4, np.float32)
+    assert x.ndim == 2 and x.shape[1] == 4
+    V = np.ascontiguousarray(viewmat, np.float32).reshape(16)
+    P = np.ascontiguousarray(projmat, np.float32).reshape(16)
+    out = np.empty((int(height), int(width)), np.float32)
+    load().pbfo_splat(int(pass_), x.ctypes.data, x.shape[0], V.ctypes.data, P.ctypes.data,
+                      int(width), int(height), out.ctypes.data)
+    return out
+
+
 def params_size() -> int:
     return int(load().pbfo_params_size())
 
@@ -215,6 +231,8 @@ def ref_load() -> C.CDLL:
         lib.pbfr_substep.restype = C.c_int
         lib.pbfr_substep_highlight.argtypes = [P, C.c_uint32, P, P, P, P, P, P, P, P]
         lib.pbfr_substep_highlight.restype = C.c_int
+        lib.pbfr_splat.argtypes = [C.c_int, P, C.c_uint32, P, P, C.c_uint32, C.c_uint32, P]
+        lib.pbfr_splat.restype = C.c_int
         _ref = lib
     return _ref
 
@@ -245,3 +263,16 @@ def ref_substep(params, x4, v4, highlight=None):
                                lam.ctypes.data, None if hl is None else hl.ctypes.data)
     return {"highlight": hl, "x": x, "v": v, "ids": ids, "start": st.reshape(g[2], g[1], g[0]),
             "end": en.reshape(g[2], g[1], g[0]), "nbr": nbr.reshape(n, 3, 4), "lambda": lam}
+
+
+def ref_splat(pass_: int, x4, viewmat, projmat, width: int, height: int):
+    """SurfaceReconstruction's particle passes through the reference's own
+    vertex/fragment shaders compiled as C++ (see ref_driver.cpp)."""
+    lib = ref_load()
+    x = np.ascontiguousarray(x4, np.float32)
+    V = np.ascontiguousarray(viewmat, np.float32).reshape(16)
+    P = np.ascontiguousarray(projmat, np.float32).reshape(16)
+    out = np.empty((int(height), int(width)), np.float32)
+    lib.pbfr_splat(int(pass_), x.ctypes.data, x.shape[0], V.ctypes.data, P.ctypes.data, int(width),
+                   int(height), out.ctypes.data)
+    return out

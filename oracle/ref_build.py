@@ -17,7 +17,8 @@ sph/updatepos, sph/update, sph/vorticity, sph/clearhighlight, sph/highlight
 (each prefixed with
 sph/foreachneighbour, as SPH's constructor compiles them, src/SPH.cpp:63-90),
 neighbourcellfinder/findcells and neighbourcells, and GetHash from
-radixsort/counting.  The radix sort's counting / blockscan / addblocksum /
+radixsort/counting; for SurfaceReconstruction's particle passes,
+particledepth/vertex + fragment and thickness/vertex.  The radix sort's counting / blockscan / addblocksum /
 globalsort kernels are not run (their workgroup barriers have no sequential
 equivalent); the driver sorts by GetHash with a stable sort over the same
 bits, which is what those kernels compute (src/RadixSort.cpp:124-133).
@@ -69,6 +70,35 @@ def translate(src: str) -> str:
     return src
 
 
+STAGE_IN = re.compile(r"layout\s*\([^)]*\)\s*in\s+(\w+)\s+(\w+)\s*;")
+STAGE_IO = re.compile(r"^[ \t]*(?:flat[ \t]+)?(?:in|out)[ \t]+(\w+)[ \t]+(\w+)[ \t]*;", re.M)
+BLOCK = re.compile(r"layout\s*\([^)]*\)\s*uniform\s+\w+\s*\{([^}]*)\}\s*;")
+DISCARD = re.compile(r"\bdiscard\s*;")
+
+
+def translate_stage(src: str) -> str:
+    """Rewrites a vertex or fragment shader's interface declarations (vertex
+    inputs, stage inputs/outputs, the uniform block) into plain variables the
+    driver sets and reads, and `discard;` into a flagged return; every body
+    stays as written."""
+    src = STAGE_IN.sub(lambda m: f"static {m.group(1)} {m.group(2)};", src)
+    src = BLOCK.sub(lambda m: " ".join(f"static {d.strip()};" for d in m.group(1).split(";")
+                                       if d.strip()), src)
+    src = STAGE_IO.sub(lambda m: f"static {m.group(1)} {m.group(2)};", src)
+    src = DISCARD.sub("{ discarded = true; return; }", src)
+    src = MAIN.sub("void main_invocation()", src)
+    return src
+
+
+# SurfaceReconstruction's particle passes (src/SurfaceReconstruction.cpp:
+# 176-231): the depth pass's two stages and the thickness pass's vertex stage
+# (its fragment stage, with noise off, only discards outside the unit disc
+# and writes 1; the driver restates that).
+STAGE_SHADERS = [("particledepth_vs", "particledepth/vertex.glsl"),
+                 ("particledepth_fs", "particledepth/fragment.glsl"),
+                 ("thickness_vs", "thickness/vertex.glsl")]
+
+
 def get_hash_function() -> str:
     """GetHash of shaders/radixsort/counting.glsl:53-57, parameter qualifier dropped."""
     src = _read("radixsort/counting.glsl")
@@ -91,6 +121,11 @@ def generate() -> str:
                      f"{body}\n}}  // namespace sh_{name}\n")
     parts.append("namespace sh_hash {\nusing namespace glsl;\nusing namespace refglobals;\n"
                  + get_hash_function() + "\n}  // namespace sh_hash\n")
+    for ns, rel in STAGE_SHADERS:
+        body = translate_stage(_read(rel))
+        parts.append(f"namespace sh_{ns} {{\nusing namespace glsl;\nstatic vec4 gl_Position;\n"
+                     f"static float gl_FragDepth;\nstatic int gl_InstanceID;\n"
+                     f"static bool discarded;\n{body}\n}}  // namespace sh_{ns}\n")
     return "\n".join(parts)
 
 

@@ -17,8 +17,19 @@ namespace glsl {
 
 typedef unsigned int uint;
 
+struct vec2;
 struct vec3;
 struct ivec3;
+
+struct vec2 {
+    float x, y;
+    vec2() : x(0), y(0) {}
+    vec2(float a, float b) : x(a), y(b) {}
+};
+inline vec2 operator*(float s, vec2 a) { return vec2(s * a.x, s * a.y); }
+inline vec2 operator+(vec2 a, vec2 b) { return vec2(a.x + b.x, a.y + b.y); }
+inline vec2 operator-(vec2 a, vec2 b) { return vec2(a.x - b.x, a.y - b.y); }
+inline float dot(vec2 a, vec2 b) { return a.x * b.x + a.y * b.y; }
 
 
 // .xyz of a 3- or 4-vector: storage shared with the vector's lanes
@@ -44,6 +55,7 @@ struct vec3 {
         return *this;
     }
     vec3(float a, float b, float c) : x(a), y(b), z(c) {}
+    vec3(vec2 a, float c) : x(a.x), y(a.y), z(c) {}
     explicit vec3(float a) : x(a), y(a), z(a) {}
     explicit vec3(const ivec3& v);
     float& operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
@@ -91,7 +103,21 @@ struct vec4 {
     vec4() : x(0), y(0), z(0), w(0) {}
     vec4(float a, float b, float c, float d) : x(a), y(b), z(c), w(d) {}
     vec4(const vec3& v, float d) : x(v.x), y(v.y), z(v.z), w(d) {}
+    vec4(vec2 v, float c, float d) : x(v.x), y(v.y), z(c), w(d) {}
 };
+inline vec4 operator+(vec4 a, vec4 b) { return vec4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+inline vec4 operator*(vec4 a, float s) { return vec4(a.x * s, a.y * s, a.z * s, a.w * s); }
+
+// mat4: four columns; mat4 * vec4 sums the column terms left to right.
+struct mat4 {
+    vec4 c[4];
+};
+inline vec4 operator*(const mat4& m, vec4 v) {
+    return vec4(((m.c[0].x * v.x + m.c[1].x * v.y) + m.c[2].x * v.z) + m.c[3].x * v.w,
+                ((m.c[0].y * v.x + m.c[1].y * v.y) + m.c[2].y * v.z) + m.c[3].y * v.w,
+                ((m.c[0].z * v.x + m.c[1].z * v.y) + m.c[2].z * v.z) + m.c[3].z * v.w,
+                ((m.c[0].w * v.x + m.c[1].w * v.y) + m.c[2].w * v.z) + m.c[3].w * v.w);
+}
 
 struct ivec4 {
     union {
@@ -116,6 +142,7 @@ inline float dot(vec3 a, vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 // GetHash (counting.glsl:56) computes the key in float (exact below 2^24).
 inline float dot(ivec3 a, ivec3 b) { return dot(vec3(a), vec3(b)); }
 inline float length(vec3 a) { return std::sqrt(dot(a, a)); }
+inline float sqrt(float a) { return std::sqrt(a); }
 inline float distance(vec3 a, vec3 b) { return length(a - b); }
 inline vec3 cross(vec3 a, vec3 b) {
     return vec3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);

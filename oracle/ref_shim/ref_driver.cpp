@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <numeric>
+#include <utility>
 #include <vector>
 
 #include "glsl.hpp"
@@ -214,6 +215,142 @@ int pbfr_substep_highlight(const Params* p, uint32_t n, float* x4, float* v4, ui
     if (out_end) std::copy(end.begin(), end.end(), out_end);
     if (out_nbr) std::copy(nbr.begin(), nbr.end(), out_nbr);
     if (out_lambda) std::copy(lambda.begin(), lambda.end(), out_lambda);
+    return 0;
+}
+
+// SurfaceReconstruction's particle passes (src/SurfaceReconstruction.cpp:
+// 176-231) with the reference's own vertex and fragment stages: pass 0 runs
+// particledepth's vertex and fragment shaders (depth test LESS, cleared to 1,
+// gl_FragDepth clamped to [0, 1]); pass 1 runs thickness's vertex shader and,
+// for its fragment stage with noise off (thickness/fragment.glsl:122-125),
+// discards outside the unit disc and adds 1 (additive blending, cleared to
+// 0).  The fixed-function steps between the stages are written out here:
+// PointSprite's quad (corners (-1, 1), (1, 1), (1, -1), (-1, -1), triangles
+// 0,2,1 and 2,0,3, src/PointSprite.cpp:33-55), the viewport transform, pixel
+// centres at i + 1/2 (row 0 at the bottom), the top-left ownership of pixel
+// centres on edges, perspective-correct interpolation and near/far clipping.
+// V, P: column-major 4x4; out: float[H][W].
+int pbfr_splat(int pass, const float* x4, uint32_t n, const float* V, const float* P, uint32_t W,
+               uint32_t H, float* out) {
+    using namespace glsl;
+    mat4 vm, pm;
+    for (int c = 0; c < 4; ++c) {
+        vm.c[c] = vec4(V[4 * c], V[4 * c + 1], V[4 * c + 2], V[4 * c + 3]);
+        pm.c[c] = vec4(P[4 * c], P[4 * c + 1], P[4 * c + 2], P[4 * c + 3]);
+    }
+    const size_t count = (size_t)W * H;
+    for (size_t k = 0; k < count; ++k) out[k] = pass == 0 ? 1.0f : 0.0f;
+    struct Corner {
+        float x, y, w, cz;
+        vec2 t;
+        vec3 p;
+    };
+    const vec2 corner[4] = {vec2(-1.0f, 1.0f), vec2(1.0f, 1.0f), vec2(1.0f, -1.0f), vec2(-1.0f, -1.0f)};
+    const float hw = 0.5f * (float)W, hh = 0.5f * (float)H;
+    auto edge = [](float ax, float ay, float bx, float by, float px, float py) {
+        return (bx - ax) * (py - ay) - (by - ay) * (px - ax);
+    };
+    auto owns = [](float ax, float ay, float bx, float by) { return (ay == by && bx < ax) || by < ay; };
+    auto in_edge = [](float e, bool own) { return e > 0.0f || (e == 0.0f && own); };
+    for (uint32_t id = 0; id < n; ++id) {
+        Corner q[4];
+        int near_out = 0, far_out = 0;
+        bool skip = false;
+        float xmin = 3.0e38f, xmax = -3.0e38f, ymin = 3.0e38f, ymax = -3.0e38f;
+        for (int k = 0; k < 4; ++k) {
+            vec4 gp;
+            vec3 fp;
+            vec2 ft;
+            if (pass == 0) {
+                namespace S = sh_particledepth_vs;
+                S::viewmat = vm;
+                S::projmat = pm;
+                S::vPosition = corner[k];
+                S::particlePosition = vec3(x4[4 * id], x4[4 * id + 1], x4[4 * id + 2]);
+                S::gl_InstanceID = (int)id;
+                S::main_invocation();
+                gp = S::gl_Position;
+                fp = S::fPosition;
+                ft = S::fTexcoord;
+            } else {
+                namespace S = sh_thickness_vs;
+                S::viewmat = vm;
+                S::projmat = pm;
+                S::vPosition = corner[k];
+                S::particlePosition = vec3(x4[4 * id], x4[4 * id + 1], x4[4 * id + 2]);
+                S::gl_InstanceID = (int)id;
+                S::main_invocation();
+                gp = S::gl_Position;
+                fp = S::fPosition;
+                ft = S::fTexcoord;
+            }
+            if (!(gp.w > 0.0f)) skip = true;
+            near_out += gp.z < -gp.w;
+            far_out += gp.z > gp.w;
+            q[k] = Corner{hw * (gp.x / gp.w) + hw, hh * (gp.y / gp.w) + hh, gp.w, gp.z, ft, fp};
+            xmin = std::fmin(xmin, q[k].x);
+            xmax = std::fmax(xmax, q[k].x);
+            ymin = std::fmin(ymin, q[k].y);
+            ymax = std::fmax(ymax, q[k].y);
+        }
+        if (skip || near_out == 4 || far_out == 4) continue;
+        const bool clip_depth = near_out > 0 || far_out > 0;
+        const float fx0 = std::ceil(xmin - 0.5f), fx1 = std::floor(xmax - 0.5f);
+        const float fy0 = std::ceil(ymin - 0.5f), fy1 = std::floor(ymax - 0.5f);
+        if (!(fx0 <= fx1) || !(fy0 <= fy1)) continue;
+        if (fx1 < 0.0f || fy1 < 0.0f || fx0 >= (float)W || fy0 >= (float)H) continue;
+        const int x0 = (int)std::fmax(fx0, 0.0f), x1 = (int)std::fmin(fx1, (float)W - 1.0f);
+        const int y0 = (int)std::fmax(fy0, 0.0f), y1 = (int)std::fmin(fy1, (float)H - 1.0f);
+        const int tri[2][3] = {{0, 2, 1}, {2, 0, 3}};
+        for (int ty = y0; ty <= y1; ++ty)
+            for (int tx = x0; tx <= x1; ++tx) {
+                const float px = (float)tx + 0.5f, py = (float)ty + 0.5f;
+                for (int t = 0; t < 2; ++t) {
+                    int i0 = tri[t][0], i1 = tri[t][1], i2 = tri[t][2];
+                    float area = edge(q[i0].x, q[i0].y, q[i1].x, q[i1].y, q[i2].x, q[i2].y);
+                    if (area == 0.0f || area != area) continue;
+                    if (area < 0.0f) {
+                        std::swap(i1, i2);
+                        area = -area;
+                    }
+                    const Corner &a = q[i0], &b = q[i1], &c = q[i2];
+                    const float e0 = edge(b.x, b.y, c.x, c.y, px, py);
+                    const float e1 = edge(c.x, c.y, a.x, a.y, px, py);
+                    const float e2 = edge(a.x, a.y, b.x, b.y, px, py);
+                    if (!in_edge(e0, owns(b.x, b.y, c.x, c.y)) || !in_edge(e1, owns(c.x, c.y, a.x, a.y)) ||
+                        !in_edge(e2, owns(a.x, a.y, b.x, b.y)))
+                        continue;
+                    const float l0 = (e0 / area) / a.w, l1 = (e1 / area) / b.w, l2 = (e2 / area) / c.w;
+                    const float ls = (l0 + l1) + l2;
+                    auto lerp = [&](float A, float B, float C) { return ((l0 * A + l1 * B) + l2 * C) / ls; };
+                    if (clip_depth) {
+                        const float zc = lerp(a.cz, b.cz, c.cz), wc = lerp(a.w, b.w, c.w);
+                        if (zc < -wc || zc > wc) break;
+                    }
+                    const vec2 tc(lerp(a.t.x, b.t.x, c.t.x), lerp(a.t.y, b.t.y, c.t.y));
+                    const size_t pix = (size_t)ty * W + tx;
+                    if (pass == 0) {
+                        namespace S = sh_particledepth_fs;
+                        S::viewmat = vm;
+                        S::projmat = pm;
+                        S::fTexcoord = tc;
+                        S::fPosition = vec3(lerp(a.p.x, b.p.x, c.p.x), lerp(a.p.y, b.p.y, c.p.y),
+                                            lerp(a.p.z, b.p.z, c.p.z));
+                        S::discarded = false;
+                        S::main_invocation();
+                        if (S::discarded) break;
+                        float d = S::gl_FragDepth;
+                        if (d != d) break;
+                        d = d < 0.0f ? 0.0f : (d > 1.0f ? 1.0f : d);
+                        if (d < out[pix]) out[pix] = d;
+                    } else {
+                        if (dot(tc, tc) > 1) break;  // thickness/fragment.glsl:122-125
+                        out[pix] += 1.0f;
+                    }
+                    break;
+                }
+            }
+    }
     return 0;
 }
 

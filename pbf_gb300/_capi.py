@@ -138,6 +138,7 @@ SIGNATURES = {
     "pbf_find_cells": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, _P]),
     "pbf_compute_diagnostics": (C.c_int, [_P, C.POINTER(Diagnostics)]),
     "pbf_highlight_neighbours": (C.c_int, [_P, _P, C.c_int]),
+    "pbf_splat": (C.c_int, [C.c_int, _P, C.c_uint32, _P, C.c_uint32, C.c_uint32, _P, _P]),
     "pbf_save_state": (C.c_int, [_P, C.c_char_p]),
     "pbf_load_state": (C.c_int, [_P, C.c_char_p]),
     "pbf_forward_record": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
