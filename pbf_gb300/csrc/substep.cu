@@ -16,6 +16,8 @@
 // its 3x3x3 stencil in the reference's order (neighbourcells.glsl:37-47),
 // each row's up-to-3-cell x-run in ascending sorted index, skipping i itself
 // (foreachneighbour.glsl:1-10), and accumulates in that order.
+#include <type_traits>
+
 #include "substep.cuh"
 #include "neighbours.cuh"
 
@@ -172,6 +174,40 @@ __device__ __forceinline__ void sweep_visit(uint32_t i, uint32_t key, const DevC
         visit_full(i, key, c, cstart, cend, body);
 }
 
+// Masked stencil scan with the pair list recorded first and the pair bodies
+// run from it afterwards: the scan writes the indices of the in-range
+// candidates (visit order) to particle i's list, then `eval` runs on the list
+// entries, read back by the same thread, so the bodies of a warp's lanes run
+// together over their own list positions (the same shape as the replaying
+// sweeps) instead of chunk by chunk.  A list longer than its capacity keeps
+// its first `cap` entries (and is marked -1 for the replaying sweep); the
+// candidates past them are found by a second scan and evaluated in order.
+template <bool LIST, class S, class F>
+__device__ __forceinline__ void scan_then_eval(uint32_t i, uint32_t key, const DevConsts& c,
+                                               const int32_t* __restrict__ cstart,
+                                               const int32_t* __restrict__ cend,
+                                               const ScanPos& X, float3 pi, const PairLists& pw,
+                                               S&& list, F&& eval) {
+    uint32_t* const out = pw.idx + i;
+    const size_t stride = pw.n;
+    uint32_t tot = 0;
+    visit_masked<LIST>(i, key, c, cstart, cend, X, pi, list, [&](uint32_t j) {
+        if (tot < pw.cap) out[(size_t)tot * stride] = j;
+        ++tot;
+    });
+    pw.cnt[i] = tot <= pw.cap ? (int32_t)tot : -1;
+    const uint32_t m = min(tot, pw.cap);
+#pragma unroll 1
+    for (uint32_t k = 0; k < m; ++k) eval(out[(size_t)k * stride]);
+    if (tot > pw.cap) {
+        uint32_t rank = 0;
+        visit_masked<false>(i, key, c, cstart, cend, X, pi, [](int32_t, uint32_t) {},
+                            [&](uint32_t j) {
+                                if (rank++ >= pw.cap) eval(j);
+                            });
+    }
+}
+
 // ---- pair bodies (shared by both visitors) ---------------------------------------
 
 struct LambdaAcc {
@@ -241,7 +277,25 @@ k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys
                 ++cnt;
             }
         };
-        if constexpr (MASKED) {
+        auto list_rec = [&](int32_t base, uint32_t lm) {
+            while (lm) {
+                const int t = __ffs(lm) - 1;
+                lm &= lm - 1;
+                if ((uint32_t)cnt < cap) nl.idx[(size_t)cnt * n + i] = (uint32_t)(base + t);
+                ++cnt;
+            }
+        };
+        auto eval = [&](uint32_t j) {
+            const float3 d = sub3(pi, xyz(__ldg(XP + j)));
+            lambda_pair(c, d, dot3(d, d), a);
+        };
+        if (MASKED && pw.cap) {
+            if (cap)
+                scan_then_eval<true>(i, skeys[i], c, cstart, cend, sx, pi, pw, list_rec, eval);
+            else
+                scan_then_eval<false>(i, skeys[i], c, cstart, cend, sx, pi, pw,
+                                      [](int32_t, uint32_t) {}, eval);
+        } else if constexpr (MASKED) {
             auto pair = [&](uint32_t j) {
                 const float3 d = sub3(pi, xyz(__ldg(XP + j)));
                 rec(j);
@@ -274,7 +328,7 @@ k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys
             });
         }
         nl.cnt[i] = (uint32_t)cnt <= cap ? cnt : -1;
-        rec.finish();
+        if (!(MASKED && pw.cap)) rec.finish();
         L[i] = make_float4(pi.x, pi.y, pi.z, lambda_finish(c, a));
         if (aux) aux[i] = lambda_aux(a);
     }
@@ -296,19 +350,25 @@ k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
     const float3 pi = xyz(P[i]);
     LambdaAcc a{0.0f, 0.0f, make_float3(0.0f, 0.0f, 0.0f)};
     PairRecorder rec{pw, i, 0u};
-    auto body = [&](uint32_t j) {
+    auto body_t = [&](uint32_t j, auto record) {
         const float3 d = sub3(pi, xyz(__ldg(P + j)));
         const float r2 = dot3(d, d);
         if (r2 > c.r2cut) return;
-        rec(j);
+        if constexpr (decltype(record)::value) rec(j);
         lambda_pair(c, d, r2, a);
     };
+    auto body = [&](uint32_t j) { body_t(j, std::true_type{}); };
     const int32_t cnt = nl.cnt[i];
-    if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot))
+    if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot)) {
         visit_list(i, cnt, nl, body);
-    else
+        rec.finish();
+    } else if (MASKED && pw.cap) {
+        scan_then_eval<false>(i, skeys[i], c, cstart, cend, sx, pi, pw, [](int32_t, uint32_t) {},
+                              [&](uint32_t j) { body_t(j, std::false_type{}); });
+    } else {
         sweep_visit<MASKED>(i, skeys[i], c, cstart, cend, sx, pi, body);
-    rec.finish();
+        rec.finish();
+    }
     L[i] = make_float4(pi.x, pi.y, pi.z, lambda_finish(c, a));
     if (aux) aux[i] = lambda_aux(a);
 }
@@ -408,11 +468,11 @@ k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
     const float3 vi = xyz(VS[i]);
     float3 acc = make_float3(0.0f, 0.0f, 0.0f), w = make_float3(0.0f, 0.0f, 0.0f);
     PairRecorder rec{pw, i, 0u};
-    auto body = [&](uint32_t j) {
+    auto body_t = [&](uint32_t j, auto record) {
         const float3 d = sub3(pi, xyz(__ldg(P + j)));  // :51
         const float r2 = dot3(d, d);
         if (r2 > c.r2cut) return;
-        rec(j);
+        if constexpr (decltype(record)::value) rec(j);
         const float len = fsqrt(r2);
         const float3 vij = sub3(xyz(__ldg(VS + j)), vi);  // :50
         acc = fma3(w_poly6(c, len), vij, acc);            // :52-54
@@ -420,12 +480,18 @@ k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
         const float3 g = scale3(d, grad_scale(c.kg, c.h, len));
         w = add3(w, cross3(vij, g));  // :55
     };
+    auto body = [&](uint32_t j) { body_t(j, std::true_type{}); };
     const int32_t cnt = nl.cnt[i];
-    if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot))
+    if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot)) {
         visit_list(i, cnt, nl, body);
-    else
+        rec.finish();
+    } else if (MASKED && pw.cap) {
+        scan_then_eval<false>(i, skeys[i], c, cstart, cend, sx, pi, pw, [](int32_t, uint32_t) {},
+                              [&](uint32_t j) { body_t(j, std::false_type{}); });
+    } else {
         sweep_visit<MASKED>(i, skeys[i], c, cstart, cend, sx, pi, body);
-    rec.finish();
+        rec.finish();
+    }
     const float3 vx = fma3(c.cx, acc, vi);  // :58
     VX[i] = make_float4(vx.x, vx.y, vx.z, 0.0f);
     OM[i] = make_float4(w.x, w.y, w.z, 0.0f);
