@@ -300,7 +300,8 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
         return cudaErrorInvalidValue;  // ensure_lists() runs before any capture
     const unsigned g = grid_for(n);
     const SweepCfg sb{s->tuning.block_size ? s->tuning.block_size : (unsigned)kBlock,
-                      s->tuning.sweep_mode == PBF_SWEEP_MASKED};
+                      s->tuning.sweep_mode == PBF_SWEEP_MASKED ? (s->pair_cap ? 2 : 1) : 0,
+                      s->tuning.use_neighbour_lists != 0};
     const uint32_t iters = s->params.num_solver_iterations;
     cudaStream_t st = s->stream;
     auto mark = [&](uint32_t idx) {

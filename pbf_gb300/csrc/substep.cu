@@ -251,11 +251,18 @@ constexpr int kSweepBlocksPerSM = 8;
 // measured ~10% slower on the 2M dam break and costs occupancy on the list
 // path, so the direct loop stays.)
 
+// Instantiations of the sweep kernels (pbf_tuning): MODE is the stencil scan
+// (kDirect: the reference's loop shape; kMasked: masked scans; kPairs: masked
+// scans recording the exact pair lists the next sweep replays), LISTS whether
+// the skin-radius neighbour lists are compiled in.  Every instantiation gives
+// the same bits.
+constexpr int kDirect = 0, kMasked = 1, kPairs = 2;
+
 // First lambda sweep of a substep (calclambda.glsl:66-102) at the predicted
 // positions XP: a full stencil scan that also records, in visit order, every
 // candidate within h + skin (the neighbour list of the later sweeps) and the
 // largest coordinate magnitude (for the guard's rounding margin).
-template <class CP, bool MASKED>
+template <class CP, int MODE, bool LISTS>
 __global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
 k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys,
                const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
@@ -268,15 +275,8 @@ k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys
         const auto& c = cp.at(i);
         pi = xyz(XP[i]);
         LambdaAcc a{0.0f, 0.0f, make_float3(0.0f, 0.0f, 0.0f)};
-        PairRecorder rec{pw, i, 0u};
         int32_t cnt = 0;
-        const uint32_t cap = c.use_lists ? nl.cap : 0u;
-        auto record = [&](uint32_t j, float r2) {
-            if (r2 <= c.r2list) {
-                if ((uint32_t)cnt < cap) nl.idx[(size_t)cnt * n + i] = j;
-                ++cnt;
-            }
-        };
+        const uint32_t cap = (LISTS && c.use_lists) ? nl.cap : 0u;
         auto list_rec = [&](int32_t base, uint32_t lm) {
             while (lm) {
                 const int t = __ffs(lm) - 1;
@@ -289,56 +289,43 @@ k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys
             const float3 d = sub3(pi, xyz(__ldg(XP + j)));
             lambda_pair(c, d, dot3(d, d), a);
         };
-        if (MASKED && pw.cap) {
-            if (cap)
+        if constexpr (MODE == kPairs) {
+            if (LISTS && cap)
                 scan_then_eval<true>(i, skeys[i], c, cstart, cend, sx, pi, pw, list_rec, eval);
             else
                 scan_then_eval<false>(i, skeys[i], c, cstart, cend, sx, pi, pw,
                                       [](int32_t, uint32_t) {}, eval);
-        } else if constexpr (MASKED) {
-            auto pair = [&](uint32_t j) {
-                const float3 d = sub3(pi, xyz(__ldg(XP + j)));
-                rec(j);
-                lambda_pair(c, d, dot3(d, d), a);
-            };
-            if (cap) {
-                visit_masked<true>(i, skeys[i], c, cstart, cend, sx, pi,
-                                   [&](int32_t base, uint32_t lm) {
-                                       while (lm) {
-                                           const int t = __ffs(lm) - 1;
-                                           lm &= lm - 1;
-                                           if ((uint32_t)cnt < cap)
-                                               nl.idx[(size_t)cnt * n + i] = (uint32_t)(base + t);
-                                           ++cnt;
-                                       }
-                                   },
-                                   pair);
-            } else {
+        } else if constexpr (MODE == kMasked) {
+            if (LISTS && cap)
+                visit_masked<true>(i, skeys[i], c, cstart, cend, sx, pi, list_rec, eval);
+            else
                 visit_masked<false>(i, skeys[i], c, cstart, cend, sx, pi,
-                                    [](int32_t, uint32_t) {}, pair);
-            }
+                                    [](int32_t, uint32_t) {}, eval);
         } else {
             visit_full(i, skeys[i], c, cstart, cend, [&](uint32_t j) {
                 const float3 d = sub3(pi, xyz(__ldg(XP + j)));
                 const float r2 = dot3(d, d);
-                record(j, r2);
+                if (LISTS && r2 <= c.r2list) {
+                    if ((uint32_t)cnt < cap) nl.idx[(size_t)cnt * n + i] = j;
+                    ++cnt;
+                }
                 if (r2 > c.r2cut) return;
-                rec(j);
                 lambda_pair(c, d, r2, a);
             });
         }
-        nl.cnt[i] = (uint32_t)cnt <= cap ? cnt : -1;
-        if (!(MASKED && pw.cap)) rec.finish();
+        if (LISTS) nl.cnt[i] = (uint32_t)cnt <= cap ? cnt : -1;
         L[i] = make_float4(pi.x, pi.y, pi.z, lambda_finish(c, a));
         if (aux) aux[i] = lambda_aux(a);
     }
-    const float m = fmaxf(fmaxf(fabsf(pi.x), fabsf(pi.y)), fabsf(pi.z));
-    warp_max_to(nl.guard, m);
+    if (LISTS) {
+        const float m = fmaxf(fmaxf(fabsf(pi.x), fabsf(pi.y)), fabsf(pi.z));
+        warp_max_to(nl.guard, m);
+    }
 }
 
 // calclambda.glsl:66-102 at positions P (iterations after the first).
 // dmax_slot: guard slot holding the largest displacement of P from XP.
-template <class CP, bool MASKED>
+template <class CP, int MODE, bool LISTS>
 __global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
 k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
          const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cstart,
@@ -349,25 +336,36 @@ k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
     const auto& c = cp.at(i);
     const float3 pi = xyz(P[i]);
     LambdaAcc a{0.0f, 0.0f, make_float3(0.0f, 0.0f, 0.0f)};
-    PairRecorder rec{pw, i, 0u};
-    auto body_t = [&](uint32_t j, auto record) {
+    auto eval = [&](uint32_t j) {
         const float3 d = sub3(pi, xyz(__ldg(P + j)));
         const float r2 = dot3(d, d);
         if (r2 > c.r2cut) return;
-        if constexpr (decltype(record)::value) rec(j);
         lambda_pair(c, d, r2, a);
     };
-    auto body = [&](uint32_t j) { body_t(j, std::true_type{}); };
-    const int32_t cnt = nl.cnt[i];
-    if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot)) {
-        visit_list(i, cnt, nl, body);
-        rec.finish();
-    } else if (MASKED && pw.cap) {
-        scan_then_eval<false>(i, skeys[i], c, cstart, cend, sx, pi, pw, [](int32_t, uint32_t) {},
-                              [&](uint32_t j) { body_t(j, std::false_type{}); });
-    } else {
-        sweep_visit<MASKED>(i, skeys[i], c, cstart, cend, sx, pi, body);
-        rec.finish();
+    bool listed = false;
+    if constexpr (LISTS) {
+        const int32_t cnt = nl.cnt[i];
+        if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot)) {
+            listed = true;
+            if constexpr (MODE == kPairs) {
+                PairRecorder rec{pw, i, 0u};
+                visit_list(i, cnt, nl, [&](uint32_t j) {
+                    const float3 d = sub3(pi, xyz(__ldg(P + j)));
+                    if (!(dot3(d, d) > c.r2cut)) rec(j);
+                    eval(j);
+                });
+                rec.finish();
+            } else {
+                visit_list(i, cnt, nl, eval);
+            }
+        }
+    }
+    if (!listed) {
+        if constexpr (MODE == kPairs)
+            scan_then_eval<false>(i, skeys[i], c, cstart, cend, sx, pi, pw, [](int32_t, uint32_t) {},
+                                  eval);
+        else
+            sweep_visit<MODE == kMasked>(i, skeys[i], c, cstart, cend, sx, pi, eval);
     }
     L[i] = make_float4(pi.x, pi.y, pi.z, lambda_finish(c, a));
     if (aux) aux[i] = lambda_aux(a);
@@ -375,7 +373,7 @@ k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
 
 // updatepos.glsl:42-104.  Reads L = (p, lambda), writes clamped positions Pn
 // and the largest displacement of Pn from XP into guard slot `out_slot`.
-template <class CP, bool MASKED>
+template <class CP, int MODE, bool LISTS>
 __global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
 k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
           const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cstart,
@@ -407,12 +405,18 @@ k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
             dp = fma3(coef, g, dp);                      // :65
         };
         const float3 xi = xyz(XP[i]);
-        if (!visit_pairs(i, pr, body)) {
-            const int32_t cnt = nl.cnt[i];
-            if (list_usable(c, nl, cnt, pi, xi, dmax_slot))
-                visit_list(i, cnt, nl, body);
-            else
-                sweep_visit<MASKED>(i, skeys[i], c, cstart, cend, sx, pi, body);
+        bool done = false;
+        if constexpr (MODE == kPairs) done = visit_pairs(i, pr, body);
+        if (!done) {
+            bool listed = false;
+            if constexpr (LISTS) {
+                const int32_t cnt = nl.cnt[i];
+                if (list_usable(c, nl, cnt, pi, xi, dmax_slot)) {
+                    visit_list(i, cnt, nl, body);
+                    listed = true;
+                }
+            }
+            if (!listed) sweep_visit<MODE != kDirect>(i, skeys[i], c, cstart, cend, sx, pi, body);
         }
         float3 q = fma3(c.oorho, dp, pi);  // :85
         // clamp (:100) as min(max(q, lo), hi) with explicit selects, so signed
@@ -425,11 +429,13 @@ k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
         q.z = (c.hi[2] < q.z) ? c.hi[2] : q.z;
         if (!finite3(q)) atomicOr(status, kDevNonFinite);
         Pn[i] = make_float4(q.x, q.y, q.z, 0.0f);
-        if (sx_out.xy) scanpos_store(sx_out, i, q.x, q.y, q.z);
-        const float3 dd = make_float3(q.x - xi.x, q.y - xi.y, q.z - xi.z);
-        disp = sqrtf(dd.x * dd.x + dd.y * dd.y + dd.z * dd.z);
+        if (MODE != kDirect) scanpos_store(sx_out, i, q.x, q.y, q.z);
+        if (LISTS) {
+            const float3 dd = make_float3(q.x - xi.x, q.y - xi.y, q.z - xi.z);
+            disp = sqrtf(dd.x * dd.x + dd.y * dd.y + dd.z * dd.z);
+        }
     }
-    warp_max_to(nl.guard + out_slot, disp);
+    if (LISTS) warp_max_to(nl.guard + out_slot, disp);
 }
 
 // update.glsl:16-28: v = (x* - x_old) / dt, x = x*, scattered back to id order.
@@ -454,7 +460,7 @@ k_commit(const float4* __restrict__ P, const uint32_t* __restrict__ perm, float4
 
 // vorticity.glsl:34-60: XSPH velocity and the vorticity vector, Jacobi
 // (every read sees the committed velocities).
-template <class CP, bool MASKED>
+template <class CP, int MODE, bool LISTS>
 __global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
 k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
               const float4* __restrict__ VS, const uint32_t* __restrict__ skeys,
@@ -467,12 +473,10 @@ k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
     const float3 pi = xyz(P[i]);
     const float3 vi = xyz(VS[i]);
     float3 acc = make_float3(0.0f, 0.0f, 0.0f), w = make_float3(0.0f, 0.0f, 0.0f);
-    PairRecorder rec{pw, i, 0u};
-    auto body_t = [&](uint32_t j, auto record) {
+    auto eval = [&](uint32_t j) {
         const float3 d = sub3(pi, xyz(__ldg(P + j)));  // :51
         const float r2 = dot3(d, d);
         if (r2 > c.r2cut) return;
-        if constexpr (decltype(record)::value) rec(j);
         const float len = fsqrt(r2);
         const float3 vij = sub3(xyz(__ldg(VS + j)), vi);  // :50
         acc = fma3(w_poly6(c, len), vij, acc);            // :52-54
@@ -480,17 +484,30 @@ k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
         const float3 g = scale3(d, grad_scale(c.kg, c.h, len));
         w = add3(w, cross3(vij, g));  // :55
     };
-    auto body = [&](uint32_t j) { body_t(j, std::true_type{}); };
-    const int32_t cnt = nl.cnt[i];
-    if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot)) {
-        visit_list(i, cnt, nl, body);
-        rec.finish();
-    } else if (MASKED && pw.cap) {
-        scan_then_eval<false>(i, skeys[i], c, cstart, cend, sx, pi, pw, [](int32_t, uint32_t) {},
-                              [&](uint32_t j) { body_t(j, std::false_type{}); });
-    } else {
-        sweep_visit<MASKED>(i, skeys[i], c, cstart, cend, sx, pi, body);
-        rec.finish();
+    bool listed = false;
+    if constexpr (LISTS) {
+        const int32_t cnt = nl.cnt[i];
+        if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot)) {
+            listed = true;
+            if constexpr (MODE == kPairs) {
+                PairRecorder rec{pw, i, 0u};
+                visit_list(i, cnt, nl, [&](uint32_t j) {
+                    const float3 d = sub3(pi, xyz(__ldg(P + j)));
+                    if (!(dot3(d, d) > c.r2cut)) rec(j);
+                    eval(j);
+                });
+                rec.finish();
+            } else {
+                visit_list(i, cnt, nl, eval);
+            }
+        }
+    }
+    if (!listed) {
+        if constexpr (MODE == kPairs)
+            scan_then_eval<false>(i, skeys[i], c, cstart, cend, sx, pi, pw, [](int32_t, uint32_t) {},
+                                  eval);
+        else
+            sweep_visit<MODE == kMasked>(i, skeys[i], c, cstart, cend, sx, pi, eval);
     }
     const float3 vx = fma3(c.cx, acc, vi);  // :58
     VX[i] = make_float4(vx.x, vx.y, vx.z, 0.0f);
@@ -500,7 +517,7 @@ k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
 
 // vorticity.glsl:65-85: confinement from the gradient of |vorticity|; writes
 // the final velocity in id order.
-template <class CP, bool MASKED>
+template <class CP, int MODE, bool LISTS>
 __global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
 k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ XP,
               const float4* __restrict__ VX, const float4* __restrict__ OM,
@@ -522,12 +539,18 @@ k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ XP,
         if (len == 0.0f) return;
         eta = fma3(Qj.w, scale3(d, grad_scale(c.kg, c.h, len)), eta);  // :72
     };
-    if (!visit_pairs(i, pr, body)) {
-        const int32_t cnt = nl.cnt[i];
-        if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot))
-            visit_list(i, cnt, nl, body);
-        else
-            sweep_visit<MASKED>(i, skeys[i], c, cstart, cend, sx, pi, body);
+    bool done = false;
+    if constexpr (MODE == kPairs) done = visit_pairs(i, pr, body);
+    if (!done) {
+        bool listed = false;
+        if constexpr (LISTS) {
+            const int32_t cnt = nl.cnt[i];
+            if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot)) {
+                visit_list(i, cnt, nl, body);
+                listed = true;
+            }
+        }
+        if (!listed) sweep_visit<MODE != kDirect>(i, skeys[i], c, cstart, cend, sx, pi, body);
     }
     if (eta_out) eta_out[i] = make_float4(eta.x, eta.y, eta.z, 0.0f);
     const float l = fsqrt(dot3(eta, eta));  // :76
@@ -618,43 +641,40 @@ void launch_keys_of(unsigned g, cudaStream_t st, const float4* x, float4* xstar,
                     uint32_t n, CP cp) {
     k_keys_of<CP><<<g, kBlock, 0, st>>>(x, xstar, keys, n, cp);
 }
+// Launches KERNEL<CP, MODE, LISTS> for the tuning in `sw`.
+#define PBF_SWEEP_LAUNCH(KERNEL, ...)                                                        \
+    do {                                                                                     \
+        const unsigned g_ = grid_for(n, (int)sw.block);                                      \
+        switch (sw.mode * 2 + (sw.lists ? 1 : 0)) {                                          \
+            case 0: KERNEL<CP, kDirect, false><<<g_, sw.block, 0, st>>>(__VA_ARGS__); break; \
+            case 1: KERNEL<CP, kDirect, true><<<g_, sw.block, 0, st>>>(__VA_ARGS__); break;  \
+            case 2: KERNEL<CP, kMasked, false><<<g_, sw.block, 0, st>>>(__VA_ARGS__); break; \
+            case 3: KERNEL<CP, kMasked, true><<<g_, sw.block, 0, st>>>(__VA_ARGS__); break;  \
+            case 4: KERNEL<CP, kPairs, false><<<g_, sw.block, 0, st>>>(__VA_ARGS__); break;  \
+            default: KERNEL<CP, kPairs, true><<<g_, sw.block, 0, st>>>(__VA_ARGS__); break;  \
+        }                                                                                    \
+    } while (0)
+
 template <class CP>
 void launch_lambda_build(SweepCfg sw, cudaStream_t st, const float4* XP, const uint32_t* skeys,
                          const int32_t* cstart, const int32_t* cend, float4* L, float4* aux,
                          NbrLists nl, PairLists pw, ScanPos sx, uint32_t n, CP cp) {
-    const unsigned g = grid_for(n, (int)sw.block);
-    if (sw.masked)
-        k_lambda_build<CP, true><<<g, sw.block, 0, st>>>(XP, skeys, cstart, cend, L, aux, nl, pw, sx,
-                                                                 n, cp);
-    else
-        k_lambda_build<CP, false><<<g, sw.block, 0, st>>>(XP, skeys, cstart, cend, L, aux, nl, pw, sx, n,
-                                                          cp);
+    PBF_SWEEP_LAUNCH(k_lambda_build, XP, skeys, cstart, cend, L, aux, nl, pw, sx, n, cp);
 }
 template <class CP>
 void launch_lambda(SweepCfg sw, cudaStream_t st, const float4* P, const float4* XP,
                    const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* L,
                    float4* aux, NbrLists nl, PairLists pw, ScanPos sx, int dmax_slot, uint32_t n,
                    CP cp) {
-    const unsigned g = grid_for(n, (int)sw.block);
-    if (sw.masked)
-        k_lambda<CP, true><<<g, sw.block, 0, st>>>(P, XP, skeys, cstart, cend, L, aux, nl, pw, sx,
-                                                           dmax_slot, n, cp);
-    else
-        k_lambda<CP, false><<<g, sw.block, 0, st>>>(P, XP, skeys, cstart, cend, L, aux, nl, pw, sx,
-                                                    dmax_slot, n, cp);
+    PBF_SWEEP_LAUNCH(k_lambda, P, XP, skeys, cstart, cend, L, aux, nl, pw, sx, dmax_slot, n, cp);
 }
 template <class CP>
 void launch_delta_p(SweepCfg sw, cudaStream_t st, const float4* L, const float4* XP,
                     const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* Pn,
                     NbrLists nl, PairLists pr, ScanPos sx, ScanPos sx_out, int dmax_slot,
                     int out_slot, uint32_t n, CP cp, uint32_t* status) {
-    const unsigned g = grid_for(n, (int)sw.block);
-    if (sw.masked)
-        k_delta_p<CP, true><<<g, sw.block, 0, st>>>(L, XP, skeys, cstart, cend, Pn, nl, pr, sx, sx_out,
-                                                            dmax_slot, out_slot, n, cp, status);
-    else
-        k_delta_p<CP, false><<<g, sw.block, 0, st>>>(L, XP, skeys, cstart, cend, Pn, nl, pr, sx, sx_out, dmax_slot,
-                                                     out_slot, n, cp, status);
+    PBF_SWEEP_LAUNCH(k_delta_p, L, XP, skeys, cstart, cend, Pn, nl, pr, sx, sx_out, dmax_slot,
+                     out_slot, n, cp, status);
 }
 template <class CP>
 void launch_commit(unsigned g, cudaStream_t st, const float4* P, const uint32_t* perm, float4* x,
@@ -666,13 +686,8 @@ void launch_vorticity_a(SweepCfg sw, cudaStream_t st, const float4* P, const flo
                         const float4* VS, const uint32_t* skeys, const int32_t* cstart,
                         const int32_t* cend, float4* VX, float4* OM, float4* Q, NbrLists nl,
                         PairLists pw, ScanPos sx, int dmax_slot, uint32_t n, CP cp) {
-    const unsigned g = grid_for(n, (int)sw.block);
-    if (sw.masked)
-        k_vorticity_a<CP, true><<<g, sw.block, 0, st>>>(P, XP, VS, skeys, cstart, cend, VX,
-                                                                OM, Q, nl, pw, sx, dmax_slot, n, cp);
-    else
-        k_vorticity_a<CP, false><<<g, sw.block, 0, st>>>(P, XP, VS, skeys, cstart, cend, VX, OM, Q,
-                                                         nl, pw, sx, dmax_slot, n, cp);
+    PBF_SWEEP_LAUNCH(k_vorticity_a, P, XP, VS, skeys, cstart, cend, VX, OM, Q, nl, pw, sx, dmax_slot,
+                     n, cp);
 }
 template <class CP>
 void launch_vorticity_b(SweepCfg sw, cudaStream_t st, const float4* Q, const float4* XP,
@@ -680,14 +695,8 @@ void launch_vorticity_b(SweepCfg sw, cudaStream_t st, const float4* Q, const flo
                         const uint32_t* perm, const int32_t* cstart, const int32_t* cend,
                         float4* v, float4* eta_out, NbrLists nl, PairLists pr, ScanPos sx,
                         int dmax_slot, uint32_t n, CP cp) {
-    const unsigned g = grid_for(n, (int)sw.block);
-    if (sw.masked)
-        k_vorticity_b<CP, true><<<g, sw.block, 0, st>>>(Q, XP, VX, OM, skeys, perm, cstart,
-                                                                cend, v, eta_out, nl, pr, sx, dmax_slot, n,
-                                                                cp);
-    else
-        k_vorticity_b<CP, false><<<g, sw.block, 0, st>>>(Q, XP, VX, OM, skeys, perm, cstart, cend, v,
-                                                         eta_out, nl, pr, sx, dmax_slot, n, cp);
+    PBF_SWEEP_LAUNCH(k_vorticity_b, Q, XP, VX, OM, skeys, perm, cstart, cend, v, eta_out, nl, pr, sx,
+                     dmax_slot, n, cp);
 }
 template <class CP>
 void launch_diagnostics(unsigned g, cudaStream_t st, const float4* P, const float4* v,

@@ -19,12 +19,14 @@ __global__ void k_find_cells(const uint32_t* __restrict__ skeys, const uint32_t*
 // OneScene and ManyScenes in substep.cu).  The neighbour-sweep launchers take
 // their block size (32..256, a multiple of 32); the others take a grid of
 // kBlock-thread blocks.
-// Launch shape of the neighbour sweeps: threads per block, and whether the
-// full-stencil scans mark in-range candidates before evaluating them
-// (visit_masked) or evaluate each where they find it (visit_full).
+// Launch shape of the neighbour sweeps: threads per block; the stencil scan
+// (0: the reference's loop shape, visit_full; 1: masked scans, visit_masked;
+// 2: masked scans that record the exact pair lists the next sweep replays);
+// whether the skin-radius neighbour lists are used.
 struct SweepCfg {
     unsigned block;
-    bool masked;
+    int mode;
+    bool lists;
 };
 
 template <class CP>
