@@ -198,12 +198,14 @@ typedef struct pbf_tuning {
                                      chunks of 32 candidates, marks the ones within h in
                                      a bit mask, then evaluates the marked ones, in the
                                      same order (a warp's lanes stay converged) */
-    uint32_t pair_list_capacity;  /* > 0: each lambda sweep records every particle's
-                                     candidates within h (in visit order, up to this
-                                     many) and the delta-p sweep over the same positions
-                                     replays them instead of scanning the stencil; the
-                                     same between the two vorticity passes.  Longer
-                                     lists fall back to the scan.  0 = off; default 64 */
+    uint32_t pair_list_capacity;  /* with PBF_SWEEP_MASKED and > 0: each lambda sweep
+                                     records every particle's candidates within h (in
+                                     visit order, up to this many), evaluates its own
+                                     pairs from that list, and the delta-p sweep over
+                                     the same positions replays it instead of scanning
+                                     the stencil; the same between the two vorticity
+                                     passes.  Longer lists fall back to scans.  0 = off;
+                                     default 64; PBF_SWEEP_DIRECT records none */
 } pbf_tuning;
 
 enum { PBF_SWEEP_DIRECT = 0, PBF_SWEEP_MASKED = 1 };
