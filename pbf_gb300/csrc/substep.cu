@@ -137,7 +137,15 @@ __device__ __forceinline__ bool visit_pairs(uint32_t i, const PairLists& pl, F&&
     const int32_t cnt = pl.cnt[i];
     if (cnt < 0) return false;
     const uint32_t* __restrict__ p = pl.idx + i;
-    for (int32_t k = 0; k < cnt; ++k) f(__ldg(p + (size_t)k * pl.n));
+    if (cnt > 0) {  // the next index is loaded one entry ahead
+        uint32_t jn = __ldg(p);
+#pragma unroll 1
+        for (int32_t k = 0; k < cnt; ++k) {
+            const uint32_t j = jn;
+            if (k + 1 < cnt) jn = __ldg(p + (size_t)(k + 1) * pl.n);
+            f(j);
+        }
+    }
     return true;
 }
 
@@ -197,8 +205,15 @@ __device__ __forceinline__ void scan_then_eval(uint32_t i, uint32_t key, const D
     });
     pw.cnt[i] = tot <= pw.cap ? (int32_t)tot : -1;
     const uint32_t m = min(tot, pw.cap);
+    if (m) {  // the next index is loaded one entry ahead
+        uint32_t jn = out[0];
 #pragma unroll 1
-    for (uint32_t k = 0; k < m; ++k) eval(out[(size_t)k * stride]);
+        for (uint32_t k = 0; k < m; ++k) {
+            const uint32_t j = jn;
+            if (k + 1 < m) jn = out[(size_t)(k + 1) * stride];
+            eval(j);
+        }
+    }
     if (tot > pw.cap) {
         uint32_t rank = 0;
         visit_masked<false>(i, key, c, cstart, cend, X, pi, [](int32_t, uint32_t) {},
