@@ -125,6 +125,97 @@ __device__ __forceinline__ float3 clamp_mask(float3 g, float3 p, const DevConsts
     return g;
 }
 
+// ---- neighbour visits of the reverse sweeps -----------------------------------
+//
+// Two reverse sweeps read each position set (delta-p then lambda at an
+// iterate, vorticity pass B then pass A at the final positions), so the first
+// scans the stencil once, writing each particle's in-range candidates (visit
+// order) to a list in the handle's pair-list buffer, and runs its pair terms
+// from that list; the second replays the list.  The lanes of a warp then run
+// their (heavy) pair terms together instead of each at its own point of the
+// stencil.  A particle whose list would overflow, or a handle without pair
+// lists, uses the direct stencil visit; results are the same either way (the
+// pair terms test r2 themselves, in the same order).
+struct AdjLists {
+    uint32_t* idx;
+    int32_t* cnt;
+    uint32_t cap, n;
+};
+
+template <class F>
+__device__ __forceinline__ void adj_replay(uint32_t i, const AdjLists& al, F&& f) {
+    const int32_t cnt = al.cnt[i];
+    const uint32_t* p = al.idx + i;
+    if (cnt > 0) {  // the next index is loaded one entry ahead
+        uint32_t jn = p[0];
+#pragma unroll 1
+        for (int32_t k = 0; k < cnt; ++k) {
+            const uint32_t j = jn;
+            if (k + 1 < cnt) jn = p[(size_t)(k + 1) * al.n];
+            f(j);
+        }
+    }
+}
+
+template <class F>
+__device__ __forceinline__ void adj_scan_eval(uint32_t i, uint32_t key, const DevConsts& c,
+                                              const int32_t* __restrict__ cstart,
+                                              const int32_t* __restrict__ cend,
+                                              const float4* __restrict__ X, float3 pi,
+                                              const AdjLists& al, F&& f) {
+    if (!al.cap) {
+        visit_full(i, key, c, cstart, cend, f);
+        return;
+    }
+    Runs r;
+    runs_of(key, c, cstart, cend, r);
+    uint32_t tot = 0;
+    uint32_t* const out = al.idx + i;
+#pragma unroll 1
+    for (int o = 0; o < 9; ++o) {
+        const int32_t e = r.e[o];
+#pragma unroll 1
+        for (int32_t base = r.b[o]; base < e; base += 32) {
+            const float4* __restrict__ p = X + base;
+            const float4* const pe = p + min(e - base, 32);
+            uint32_t m = 0, bit = 1;
+#pragma unroll 1
+            for (; p < pe; ++p) {
+                const float4 xj = __ldg(p);
+                const float3 d = make_float3(pi.x - xj.x, pi.y - xj.y, pi.z - xj.z);
+                if (!(d.x * d.x + d.y * d.y + d.z * d.z > c.r2cut)) m |= bit;
+                bit <<= 1;
+            }
+            const uint32_t self = i - (uint32_t)base;
+            if (self < 32u) m &= ~(1u << self);
+            while (m) {
+                const int t = __ffs(m) - 1;
+                m &= m - 1;
+                if (tot < al.cap) out[(size_t)tot * al.n] = (uint32_t)(base + t);
+                ++tot;
+            }
+        }
+    }
+    if (tot <= al.cap) {
+        al.cnt[i] = (int32_t)tot;
+        adj_replay(i, al, f);
+    } else {
+        al.cnt[i] = -1;
+        visit_full(i, key, c, cstart, cend, f);
+    }
+}
+
+template <class F>
+__device__ __forceinline__ void adj_visit_again(uint32_t i, uint32_t key, const DevConsts& c,
+                                                const int32_t* __restrict__ cstart,
+                                                const int32_t* __restrict__ cend,
+                                                const AdjLists& al, F&& f) {
+    if (al.cap && al.cnt[i] >= 0)
+        adj_replay(i, al, f);
+    else
+        visit_full(i, key, c, cstart, cend, f);
+}
+
 // Constants of particle `id` (scene lookup by id for batches).
 template <class CP>
 __device__ __forceinline__ const DevConsts& consts_of(const CP& cp, uint32_t id) {
@@ -171,7 +262,7 @@ k_adj_vort_b2(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ sk
               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
               const float4* __restrict__ Q, const float4* __restrict__ OM,
               const float4* __restrict__ ETB, float4* __restrict__ OMB, float4* __restrict__ PA,
-              uint32_t n, CP cp) {
+              AdjLists al, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t id = perm[i];
@@ -182,7 +273,7 @@ k_adj_vort_b2(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ sk
     const float3 ebi = f3(ETB[i]);
     float mb = 0.0f;
     float3 pb = make_float3(0.0f, 0.0f, 0.0f);
-    visit_full(i, skeys[i], c, cstart, cend, [&](uint32_t j) {
+    adj_scan_eval(i, skeys[i], c, cstart, cend, Q, pi, al, [&](uint32_t j) {
         const float4 Qj = __ldg(Q + j);
         const float3 d = pi - f3(Qj);
         const float r2 = dotf(d, d);
@@ -207,7 +298,7 @@ k_adj_vort_a(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ ske
              const float4* __restrict__ PF, const float4* __restrict__ VS,
              const float4* __restrict__ VSB, const float4* __restrict__ OMB,
              float4* __restrict__ VCB, float4* __restrict__ PA, double* __restrict__ acc_c,
-             uint32_t n, CP cp) {
+             AdjLists al, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t id = perm[i];
@@ -219,7 +310,7 @@ k_adj_vort_a(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ ske
     float3 vb = sbi;
     float3 pb = f3(PA[i]);
     float3 wsum = make_float3(0.0f, 0.0f, 0.0f);
-    visit_full(i, skeys[i], c, cstart, cend, [&](uint32_t j) {
+    adj_visit_again(i, skeys[i], c, cstart, cend, al, [&](uint32_t j) {
         const float3 d = pi - f3(__ldg(PF + j));
         const float r2 = dotf(d, d);
         if (r2 > c.r2cut) return;
@@ -276,7 +367,8 @@ k_adj_delta_p(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ sk
               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
               const float4* __restrict__ L, const float4* __restrict__ AUX,
               const float4* __restrict__ QB, float4* __restrict__ PDB, float4* __restrict__ RS,
-              double* __restrict__ acc_eps, double* __restrict__ acc_k, uint32_t n, CP cp) {
+              double* __restrict__ acc_eps, double* __restrict__ acc_k, AdjLists al, uint32_t n,
+              CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t id = perm[i];
@@ -288,7 +380,7 @@ k_adj_delta_p(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ sk
     float lb = 0.0f, kb = 0.0f;
     float3 pb = qbi;
     const float sc4 = c.scale * c.scale * c.scale * c.scale;
-    visit_full(i, skeys[i], c, cstart, cend, [&](uint32_t j) {
+    adj_scan_eval(i, skeys[i], c, cstart, cend, L, pi, al, [&](uint32_t j) {
         const float4 Lj = __ldg(L + j);
         const float3 d = pi - f3(Lj);
         const float r2 = dotf(d, d);
@@ -327,7 +419,8 @@ k_adj_lambda(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ ske
              const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
              const float4* __restrict__ L, const float4* __restrict__ AUX,
              const float4* __restrict__ RS, const float4* __restrict__ PDB,
-             float4* __restrict__ QB, float4* __restrict__ XSB, int first, uint32_t n, CP cp) {
+             float4* __restrict__ QB, float4* __restrict__ XSB, int first, AdjLists al, uint32_t n,
+             CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t id = perm[i];
@@ -336,7 +429,7 @@ k_adj_lambda(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ ske
     const float4 RSi = RS[i];
     const float3 gi = f3(AUX[i]);
     float3 pb = f3(PDB[i]);
-    visit_full(i, skeys[i], c, cstart, cend, [&](uint32_t j) {
+    adj_visit_again(i, skeys[i], c, cstart, cend, al, [&](uint32_t j) {
         const float3 d = pi - f3(__ldg(L + j));
         const float r2 = dotf(d, d);
         if (r2 > c.r2cut) return;
@@ -430,23 +523,24 @@ cudaError_t reverse_substep(pbf_sim* s, Tape* t, const Tape::Slot& sl, const CP&
     double* acc_k = t->acc + n;
     double* acc_c = t->acc + 2 * (size_t)n;
     double* acc_ev = t->acc + 3 * (size_t)n;
+    const AdjLists al{s->pair_idx, s->pair_cnt, s->pair_cap, n};
     if (t->vort) {
         k_adj_vort_b1<<<g, kAdjBlock, 0, st>>>(sl.perm, t->VB, sl.OM, sl.ETA, t->VSB, t->ETB,
                                                t->OMB, acc_ev, n, cp);
         k_adj_vort_b2<<<g, kAdjBlock, 0, st>>>(sl.perm, sl.skeys, sl.cstart, sl.cend, sl.Q, sl.OM,
-                                               t->ETB, t->OMB, t->PA, n, cp);
+                                               t->ETB, t->OMB, t->PA, al, n, cp);
         k_adj_vort_a<<<g, kAdjBlock, 0, st>>>(sl.perm, sl.skeys, sl.cstart, sl.cend, sl.PF, sl.VS,
-                                              t->VSB, t->OMB, t->VCB, t->PA, acc_c, n, cp);
+                                              t->VSB, t->OMB, t->VCB, t->PA, acc_c, al, n, cp);
     }
     k_adj_commit<<<g, kAdjBlock, 0, st>>>(sl.perm, t->XB, t->VB, t->VCB, t->PA, sl.PF, t->QB,
                                           t->XOB, t->XSB, t->vort ? 1 : 0, iters, n, cp);
     for (int k = iters - 1; k >= 0; --k) {
         k_adj_delta_p<<<g, kAdjBlock, 0, st>>>(sl.perm, sl.skeys, sl.cstart, sl.cend, sl.L[k],
-                                               sl.AUX[k], t->QB, t->PDB, t->RS, acc_eps, acc_k, n,
-                                               cp);
+                                               sl.AUX[k], t->QB, t->PDB, t->RS, acc_eps, acc_k, al,
+                                               n, cp);
         k_adj_lambda<<<g, kAdjBlock, 0, st>>>(sl.perm, sl.skeys, sl.cstart, sl.cend, sl.L[k],
                                               sl.AUX[k], t->RS, t->PDB, t->QB, t->XSB,
-                                              k == 0 ? 1 : 0, n, cp);
+                                              k == 0 ? 1 : 0, al, n, cp);
     }
     k_adj_predict<<<g, kAdjBlock, 0, st>>>(t->XSB, t->XOB, t->XB2, t->VB2, n, cp);
     std::swap(t->XB, t->XB2);

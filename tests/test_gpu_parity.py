@@ -233,12 +233,16 @@ def test_set_params_rejects_grid_change(gpu):
                                     dict(use_neighbour_lists=True, skin_h=0.0, sweep_mode="masked"),
                                     dict(pair_list_capacity=0),
                                     dict(pair_list_capacity=1, sweep_mode="direct"),
+                                    dict(pair_list_capacity=1, sweep_mode="masked"),
                                     dict(pair_list_capacity=20, use_neighbour_lists=False),
-                                    dict(pair_list_capacity=4096, use_neighbour_lists=True)])
+                                    dict(pair_list_capacity=33, block_size=64),
+                                    dict(pair_list_capacity=4096, use_neighbour_lists=True),
+                                    dict(pair_list_capacity=8, use_neighbour_lists=True, skin_h=0.3)])
 def test_tuning_never_changes_results(gpu, oracle_mod, tuning):
     """Neighbour lists, their capacity and skin, the sweep mode and the pair
-    lists (capacity 1 and 20 overflow often, falling back to the scan) are
-    performance knobs only."""
+    lists (capacities 1, 8 and 20 overflow often: the scanning sweep then
+    finds the entries past the capacity with a second scan, and the replaying
+    sweep falls back to a scan) are performance knobs only."""
     sc = scenes.plain_16k()
     g = pg.SPH(sc.n, tuple(sc.params.grid), sc.params)
     g.set_tuning(**tuning)
