@@ -65,6 +65,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-scene comparison")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the backward/forward ratio")
     ap.add_argument("--no-splat", action="store_true", help="skip the depth/thickness splatting leg")
+    ap.add_argument("--no-small", action="store_true", help="skip the 16,384-particle configuration")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--recovery", action="store_true",
                     help="also run the 64-scene parameter recovery (about a minute)")
@@ -386,6 +387,50 @@ def recovery(stream, num_scenes: int = 64, substeps: int = 32, steps: int = 50, 
             "note": "errors are mean |theta - hidden| / range (0.015 for c, 0.001 for eps_v)"}
 
 
+def small_config(stream, with_cpu: bool):
+    """The reference's CPU-runnable configuration: the 16,384-particle dam break
+    (32x16x32 lattice in a 64^3 box, 3 iterations), its full 200 substeps on
+    the GPU (graph replay, timed per 50 substeps: with epsilon = 0.01 the
+    scene collapses into dense clumps after ~60 substeps, where every
+    particle has thousands of neighbours and 16,384 threads cannot fill the
+    GPU) and, when asked, through the FP32 oracle on the host cores."""
+    import torch
+    import pbf_gb300 as pg
+    from pbf_gb300 import scenes
+    sc = scenes.plain_16k()
+    it = sc.params.num_solver_iterations
+    sim = pg.SPH(sc.n, tuple(sc.params.grid), sc.params)
+    sim.set_stream(stream.cuda_stream)
+    sim.set_state(sc.x4, sc.v4)
+    sim.step(3)
+    sim.set_state(sc.x4, sc.v4)
+    torch.cuda.synchronize()
+    seg = 50
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(sc.substeps // seg + 1)]
+    ev[0].record(stream)
+    for k in range(sc.substeps // seg):
+        sim.step(seg)
+        ev[k + 1].record(stream)
+    torch.cuda.synchronize()
+    ms = ev[0].elapsed_time(ev[-1])
+    res = {"workload": sc.name, "particles": sc.n, "solver_iterations": it,
+           "substeps": sc.substeps, "ms_per_step": ms / sc.substeps,
+           "value": sc.n * it * sc.substeps / (ms * 1e-3), "unit": UNIT,
+           "ms_per_step_by_50": [ev[k].elapsed_time(ev[k + 1]) / seg for k in range(len(ev) - 1)]}
+    sim.close()
+    if with_cpu:
+        import oracle
+        o = oracle.Oracle(sc.params, sc.n)
+        o.set_state(sc.x4, sc.v4)
+        secs = o.step(sc.substeps)
+        res["cpu_oracle"] = {"value": sc.n * it * sc.substeps / secs, "unit": UNIT,
+                             "cores": oracle.max_threads(), "seconds": secs}
+        o.set_state(sc.x4, sc.v4)
+        secs50 = o.step(seg)
+        res["cpu_oracle"]["first_50_value"] = sc.n * it * seg / secs50
+    return res
+
+
 def cpu_baseline(scene, substeps: int):
     """FP32 oracle on all host threads, `substeps` full substeps of the scene."""
     import oracle
@@ -597,6 +642,9 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(scene, args.cpu_substeps)
+    small = None
+    if not args.no_small:
+        small = small_config(stream, rank == 0 and world == 1 and not args.no_cpu_baseline)
 
     if rank == 0:
         line = {
@@ -625,6 +673,7 @@ def main():
             "batched_256": batched,
             "adjoint_32k": adjoint,
             "splat_reference_scene": splats,
+            "dam_break_16k_200": small,
             "recovery_64": recov,
             "clocks": clk,
             "cpu_baseline": cpu,
