@@ -205,7 +205,7 @@ typedef struct pbf_tuning {
                                      the same positions replays it instead of scanning
                                      the stencil; the same between the two vorticity
                                      passes.  Longer lists fall back to scans.  0 = off;
-                                     default 64; PBF_SWEEP_DIRECT records none */
+                                     default 128; PBF_SWEEP_DIRECT records none */
 } pbf_tuning;
 
 enum { PBF_SWEEP_DIRECT = 0, PBF_SWEEP_MASKED = 1 };

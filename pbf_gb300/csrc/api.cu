@@ -147,7 +147,7 @@ pbf_tuning default_tuning() {
     t.skin_h = 0.15f;
     t.block_size = 256;
     t.sweep_mode = PBF_SWEEP_MASKED;
-    t.pair_list_capacity = 64;
+    t.pair_list_capacity = 128;
     return t;
 }
 
