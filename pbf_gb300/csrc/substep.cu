@@ -11,6 +11,8 @@
 //   Q             float4[n]  sorted (x, y, z, |vorticity|) for the confinement pass
 //   cell_start    i32[cells] first sorted index of each cell, -1 when empty
 //   cell_end      i32[cells] one past the last sorted index (valid where start != -1)
+//   scan copies   ScanPos    pair-interleaved copies of XP and the iterates (masked scans)
+//   pair lists    u32[cap][n] in-range candidates per particle, SoA (PairLists)
 //
 // Every neighbour sweep visits, for sorted particle i, the 9 (dy, dz) rows of
 // its 3x3x3 stencil in the reference's order (neighbourcells.glsl:37-47),
@@ -22,10 +24,6 @@
 #include "neighbours.cuh"
 
 namespace pbf {
-
-namespace {
-
-}  // namespace
 
 // predictpos.glsl:18-38 fused with the cell key of GetHash (counting.glsl:53-57).
 template <class CP>
@@ -258,13 +256,10 @@ __device__ __forceinline__ float lambda_finish(const DevConsts& c, const LambdaA
 // ---- solver kernels --------------------------------------------------------------
 
 // Resident 256-thread blocks per SM the sweep kernels are compiled for (caps
-// them at 32 registers: full occupancy hides the gather and sqrt/div latency).
+// them at 32 registers: full occupancy hides the gather and sqrt/div latency;
+// 6 or 4 blocks with more registers measured slower).  One thread per sorted
+// particle.
 constexpr int kSweepBlocksPerSM = 8;
-//
-// One thread per sorted particle; each walks its own candidates directly.
-// (A warp-lockstep scan with a shared-memory queue of in-range candidates was
-// measured ~10% slower on the 2M dam break and costs occupancy on the list
-// path, so the direct loop stays.)
 
 // Instantiations of the sweep kernels (pbf_tuning): MODE is the stencil scan
 // (kDirect: the reference's loop shape; kMasked: masked scans; kPairs: masked
