@@ -544,6 +544,8 @@ def main():
     ms = float(t.item())
     launches = sim.kernels_per_substep() * K
     value = world * scene.n * it * K / (ms * 1e-3)
+    # the state at the end of the timed window (outside the timed region)
+    state_after = sim.diagnostics()
 
     # per-kernel durations (eager, events per kernel) over the first
     # min(K, 50) substeps of the same window
@@ -674,6 +676,7 @@ def main():
             "adjoint_32k": adjoint,
             "splat_reference_scene": splats,
             "dam_break_16k_200": small,
+            "state_after_window": state_after,
             "recovery_64": recov,
             "clocks": clk,
             "cpu_baseline": cpu,

@@ -33,6 +33,7 @@
 //   v_i = (p_i - x_i)/dt;  vs_i = v_i + c sum_j W_ij (v_j - v_i);  w_i = sum_j (v_j - v_i) x G_ij
 //   eta_i = sum_j |w_j| G_ij;  N_i = eta_i/|eta_i|;  vf_i = vs_i + dt eps_v (N_i x w_i)
 #include "neighbours.cuh"
+#include "internal.h"
 #include "sim.h"
 
 #include <algorithm>
@@ -601,6 +602,7 @@ using namespace pbf;
 extern "C" {
 
 pbf_status pbf_forward_record(pbf_sim* s, uint32_t substeps, uint32_t checkpoint_every) {
+    NvtxRange nvtx_("pbf_forward_record");
     if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
     if (substeps == 0 || checkpoint_every == 0)
         return fail(s, PBF_ERR_INVALID_ARGUMENT, "substeps and checkpoint_every must be positive");
@@ -635,6 +637,7 @@ pbf_status pbf_forward_record(pbf_sim* s, uint32_t substeps, uint32_t checkpoint
 
 pbf_status pbf_backward(pbf_sim* s, const float* dL_dx4, const float* dL_dv4, int where,
                         float* dL_dx0_4, float* dL_dv0_4, pbf_param_grads* grads) {
+    NvtxRange nvtx_("pbf_backward");
     if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
     if (!s->tape) return fail(s, PBF_ERR_INVALID_ARGUMENT, "no recorded forward run (pbf_forward_record)");
     if (where != PBF_HOST && where != PBF_DEVICE) return fail(s, PBF_ERR_INVALID_ARGUMENT, "bad where");

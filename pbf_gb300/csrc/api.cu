@@ -251,6 +251,7 @@ pbf_status timed_substep(pbf_sim* s);
 
 
 pbf_status timed_substep(pbf_sim* s) {
+    NvtxRange nvtx_("timed substep");
     const uint32_t iters = s->params.num_solver_iterations;
     const size_t need = 7 + 2 * (size_t)iters;
     while (s->ev.size() < need) {
@@ -601,6 +602,7 @@ pbf_status pbf_set_tuning(pbf_sim* s, const pbf_tuning* t) {
 }
 
 pbf_status pbf_autotune(pbf_sim* s, uint32_t trial_substeps, pbf_tuning* best) {
+    NvtxRange nvtx_("pbf_autotune");
     if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
     if (trial_substeps == 0) return fail(s, PBF_ERR_INVALID_ARGUMENT, "trial_substeps must be positive");
     DeviceGuard dg(s->device);
@@ -708,6 +710,7 @@ pbf_status pbf_set_stream(pbf_sim* s, void* stream) {
 }
 
 pbf_status pbf_set_state(pbf_sim* s, const float* x4, const float* v4, int where) {
+    NvtxRange nvtx_("pbf_set_state");
     if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
     if (!x4 || !v4) return fail(s, PBF_ERR_INVALID_ARGUMENT, "x4 and v4 are required");
     if (where != PBF_HOST && where != PBF_DEVICE) return fail(s, PBF_ERR_INVALID_ARGUMENT, "bad where");
@@ -720,6 +723,7 @@ pbf_status pbf_set_state(pbf_sim* s, const float* x4, const float* v4, int where
 }
 
 pbf_status pbf_get_state(pbf_sim* s, float* x4, float* v4, int where) {
+    NvtxRange nvtx_("pbf_get_state");
     if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
     if (where != PBF_HOST && where != PBF_DEVICE) return fail(s, PBF_ERR_INVALID_ARGUMENT, "bad where");
     DeviceGuard dg(s->device);
@@ -737,6 +741,7 @@ pbf_status pbf_device_buffers(pbf_sim* s, float** x4, float** v4) {
 }
 
 pbf_status pbf_step(pbf_sim* s, uint32_t substeps) {
+    NvtxRange nvtx_("pbf_step");
     if (!s) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "sim is NULL");
     DeviceGuard dg(s->device);
     if (s->timing) {
@@ -851,6 +856,7 @@ pbf_status pbf_get_solver(pbf_sim* s, float* lambda_sorted, float* xpred4_sorted
 }
 
 pbf_status pbf_compute_diagnostics(pbf_sim* s, pbf_diagnostics* out) {
+    NvtxRange nvtx_("pbf_compute_diagnostics");
     if (!s || !out) return fail(s, PBF_ERR_INVALID_ARGUMENT, "NULL argument");
     DeviceGuard dg(s->device);
     const uint32_t n = s->n;

@@ -25,6 +25,7 @@
 #include <stdint.h>
 
 #include "../../include/pbf.h"
+#include "internal.h"
 #include "sim.h"
 
 namespace pbf {
@@ -194,6 +195,7 @@ __global__ void k_fill(float* __restrict__ out, size_t count, float value) {
 
 extern "C" pbf_status pbf_splat(int pass, const float* positions, uint32_t n, const pbf_view* view,
                                 uint32_t width, uint32_t height, float* out, void* stream) {
+    pbf::NvtxRange nvtx_("pbf_splat");
     using namespace pbf;
     if (pass != PBF_SPLAT_DEPTH && pass != PBF_SPLAT_THICKNESS)
         return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "pass must be PBF_SPLAT_DEPTH or PBF_SPLAT_THICKNESS");
