@@ -667,7 +667,10 @@ def main():
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "alg_bytes_per_launch": ALG_BYTES[dom] * scene.n,
                          "ms_per_launch": per_launch[dom],
-                         "note": "neighbour sweeps are FP32-issue / L1-gather bound, not HBM"},
+                         "issue_active": (prof or {}).get("issue_active", {}).get(dom),
+                         "note": "neighbour sweeps are bound by instruction issue (issue_active: "
+                                 "share of issue slots used, from the committed ncu capture) and "
+                                 "gather latency, not by HBM"},
             "kernel_ms_per_substep": {k: v / counted for k, v in stages.items()},
             "kernel_share": {k: v / total_stage for k, v in stages.items()},
             "gpu_launches": launches,
