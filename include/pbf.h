@@ -197,7 +197,12 @@ typedef struct pbf_tuning {
                                      PBF_SWEEP_MASKED (default): it scans each run in
                                      chunks of 32 candidates, marks the ones within h in
                                      a bit mask, then evaluates the marked ones, in the
-                                     same order (a warp's lanes stay converged) */
+                                     same order (a warp's lanes stay converged);
+                                     PBF_SWEEP_COOP: a warp per particle, its lanes
+                                     testing 32 candidates at once and computing their
+                                     pair terms in parallel, folded in the same order
+                                     (for scenes too small to fill the GPU with a
+                                     thread per particle, and clumped states) */
     uint32_t pair_list_capacity;  /* with PBF_SWEEP_MASKED and > 0: each lambda sweep
                                      records every particle's candidates within h (in
                                      visit order, up to this many), evaluates its own
@@ -208,7 +213,7 @@ typedef struct pbf_tuning {
                                      default 128; PBF_SWEEP_DIRECT records none */
 } pbf_tuning;
 
-enum { PBF_SWEEP_DIRECT = 0, PBF_SWEEP_MASKED = 1 };
+enum { PBF_SWEEP_DIRECT = 0, PBF_SWEEP_MASKED = 1, PBF_SWEEP_COOP = 2 };
 
 /* No reference counterpart (the reference has no tuning surface). */
 pbf_status pbf_set_tuning(pbf_sim* sim, const pbf_tuning* tuning);

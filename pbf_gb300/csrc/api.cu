@@ -301,7 +301,9 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
         return cudaErrorInvalidValue;  // ensure_lists() runs before any capture
     const unsigned g = grid_for(n);
     const SweepCfg sb{s->tuning.block_size ? s->tuning.block_size : (unsigned)kBlock,
-                      s->tuning.sweep_mode == PBF_SWEEP_MASKED ? (s->pair_cap ? 2 : 1) : 0,
+                      s->tuning.sweep_mode == PBF_SWEEP_MASKED ? (s->pair_cap ? 2 : 1)
+                      : s->tuning.sweep_mode == PBF_SWEEP_COOP ? 3
+                                                               : 0,
                       s->tuning.use_neighbour_lists != 0};
     const uint32_t iters = s->params.num_solver_iterations;
     cudaStream_t st = s->stream;
@@ -586,8 +588,10 @@ pbf_status pbf_set_tuning(pbf_sim* s, const pbf_tuning* t) {
         return fail(s, PBF_ERR_INVALID_ARGUMENT, "block_size must be 0 or a multiple of 32 in [32, 256]");
     if (t->pair_list_capacity > 4096)
         return fail(s, PBF_ERR_INVALID_ARGUMENT, "pair_list_capacity must be in [0, 4096]");
-    if (t->sweep_mode != PBF_SWEEP_DIRECT && t->sweep_mode != PBF_SWEEP_MASKED)
-        return fail(s, PBF_ERR_INVALID_ARGUMENT, "sweep_mode must be PBF_SWEEP_DIRECT or PBF_SWEEP_MASKED");
+    if (t->sweep_mode != PBF_SWEEP_DIRECT && t->sweep_mode != PBF_SWEEP_MASKED &&
+        t->sweep_mode != PBF_SWEEP_COOP)
+        return fail(s, PBF_ERR_INVALID_ARGUMENT,
+                    "sweep_mode must be PBF_SWEEP_DIRECT, PBF_SWEEP_MASKED or PBF_SWEEP_COOP");
     DeviceGuard dg(s->device);
     PBF_CUDA(s, cudaStreamSynchronize(s->stream));
     s->tuning = *t;
@@ -646,6 +650,12 @@ pbf_status pbf_autotune(pbf_sim* s, uint32_t trial_substeps, pbf_tuning* best) {
                 cand.push_back(t);
             }
         }
+    {
+        pbf_tuning t = original;  // the warp-cooperative sweeps (block size and lists unused)
+        t.sweep_mode = PBF_SWEEP_COOP;
+        t.use_neighbour_lists = 0;
+        cand.push_back(t);
+    }
     float best_ms = 1e30f;
     pbf_tuning best_t = original;
     pbf_status r = PBF_OK;

@@ -448,6 +448,211 @@ k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
     if (LISTS) warp_max_to(nl.guard + out_slot, disp);
 }
 
+// ---- warp-cooperative sweeps (sweep_mode PBF_SWEEP_COOP) ---------------------------
+//
+// One warp per sorted particle i, for scenes too small to fill the GPU with a
+// thread per particle (and for clumped states, where each particle has
+// thousands of neighbours): the lanes test 32 consecutive candidates of a run
+// at once (coalesced loads), each in-range lane computes its pair term, and
+// every lane then folds the terms into the particle's sums in ascending
+// candidate order, reading them from the owning lanes by shuffles.  The terms
+// are the same functions and the folding order the same visit order as the
+// one-thread sweeps, so the bits are the same.
+constexpr int kCoop = 3;
+constexpr uint32_t kFull = 0xFFFFFFFFu;
+
+__device__ __forceinline__ float shf(float v, int src) { return __shfl_sync(kFull, v, src); }
+__device__ __forceinline__ float3 shf3(float3 v, int src) {
+    return make_float3(shf(v.x, src), shf(v.y, src), shf(v.z, src));
+}
+
+// Calls term(j, d, r2) on every in-range candidate's own lane (returning
+// whether the candidate has a term), then fold(src_lane) on all lanes for
+// each in-range candidate with a term, in visit order.
+template <class T, class Fo>
+__device__ __forceinline__ void coop_visit(uint32_t i, uint32_t key, const DevConsts& c,
+                                           const int32_t* __restrict__ cstart,
+                                           const int32_t* __restrict__ cend,
+                                           const float4* __restrict__ X, float3 pi, T&& term,
+                                           Fo&& fold) {
+    const uint32_t lane = threadIdx.x & 31u;
+    Runs r;
+    runs_of(key, c, cstart, cend, r);
+#pragma unroll 1
+    for (int o = 0; o < 9; ++o) {
+        const int32_t e = r.e[o];
+#pragma unroll 1
+        for (int32_t base = r.b[o]; base < e; base += 32) {
+            const uint32_t j = (uint32_t)base + lane;
+            bool has = false;
+            if ((int32_t)j < e && j != i) {
+                const float3 d = sub3(pi, xyz(__ldg(X + j)));
+                const float r2 = dot3(d, d);
+                if (!(r2 > c.r2cut)) has = term(j, d, r2);
+            }
+            uint32_t m = __ballot_sync(kFull, has);
+            while (m) {
+                const int src = __ffs(m) - 1;
+                m &= m - 1;
+                fold(src);
+            }
+        }
+    }
+}
+
+template <class CP>
+__global__ void __launch_bounds__(kBlock)
+k_lambda_coop(const float4* __restrict__ P, const uint32_t* __restrict__ skeys,
+              const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
+              float4* __restrict__ L, float4* __restrict__ aux, uint32_t n, CP cp) {
+    const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= n) return;  // whole warps: n and the lane count agree per warp
+    const auto& c = cp.at(i);
+    const float3 pi = xyz(P[i]);
+    LambdaAcc a{0.0f, 0.0f, make_float3(0.0f, 0.0f, 0.0f)};
+    float tw = 0.0f, tgg = 0.0f;
+    float3 tg = make_float3(0.0f, 0.0f, 0.0f);
+    bool tgrad = false;
+    coop_visit(i, skeys[i], c, cstart, cend, P, pi,
+               [&](uint32_t, float3 d, float r2) {
+                   const float len = fsqrt(r2);
+                   tw = w_poly6(c, len);
+                   tgrad = len != 0.0f;
+                   if (tgrad) {
+                       tg = scale3(d, grad_scale(c.kg_lambda, c.h, len));
+                       tgg = dot3(tg, tg);
+                   }
+                   return true;
+               },
+               [&](int src) {
+                   a.rho = fadd(a.rho, shf(tw, src));  // calclambda.glsl:80-82
+                   const bool g = __shfl_sync(kFull, tgrad, src);
+                   const float gg = shf(tgg, src);
+                   const float3 gv = shf3(tg, src);
+                   if (g) {
+                       a.sumk = fadd(a.sumk, gg);  // :89
+                       a.gi = add3(a.gi, gv);       // :93
+                   }
+               });
+    if ((threadIdx.x & 31u) == 0u) {
+        L[i] = make_float4(pi.x, pi.y, pi.z, lambda_finish(c, a));
+        if (aux) aux[i] = lambda_aux(a);
+    }
+}
+
+template <class CP>
+__global__ void __launch_bounds__(kBlock)
+k_delta_p_coop(const float4* __restrict__ L, const uint32_t* __restrict__ skeys,
+               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
+               float4* __restrict__ Pn, uint32_t n, CP cp, uint32_t* status) {
+    const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= n) return;
+    const auto& c = cp.at(i);
+    const float4 Li = L[i];
+    const float3 pi = xyz(Li);
+    const float li = Li.w;
+    float3 dp = make_float3(0.0f, 0.0f, 0.0f);
+    float tcoef = 0.0f;
+    float3 tg = make_float3(0.0f, 0.0f, 0.0f);
+    coop_visit(i, skeys[i], c, cstart, cend, L, pi,
+               [&](uint32_t j, float3 d, float r2) {
+                   const float len = fsqrt(r2);
+                   if (len == 0.0f) return false;
+                   float sc = fmul(c.scale, w_poly6(c, len));  // updatepos.glsl:57
+                   sc = fmul(sc, sc);                           // :58
+                   sc = fmul(sc, sc);                           // :59
+                   sc = fmul(c.negk, sc);                       // :60
+                   tcoef = fadd(fadd(li, __ldg(L + j).w), sc);  // :65
+                   tg = scale3(d, grad_scale(c.kg, c.h, len));
+                   return true;
+               },
+               [&](int src) { dp = fma3(shf(tcoef, src), shf3(tg, src), dp); });  // :65
+    if ((threadIdx.x & 31u) == 0u) {
+        float3 q = fma3(c.oorho, dp, pi);  // :85
+        q.x = (q.x < c.lo[0]) ? c.lo[0] : q.x;
+        q.x = (c.hi[0] < q.x) ? c.hi[0] : q.x;
+        q.y = (q.y < c.lo[1]) ? c.lo[1] : q.y;
+        q.y = (c.hi[1] < q.y) ? c.hi[1] : q.y;
+        q.z = (q.z < c.lo[2]) ? c.lo[2] : q.z;
+        q.z = (c.hi[2] < q.z) ? c.hi[2] : q.z;
+        if (!finite3(q)) atomicOr(status, kDevNonFinite);
+        Pn[i] = make_float4(q.x, q.y, q.z, 0.0f);
+    }
+}
+
+template <class CP>
+__global__ void __launch_bounds__(kBlock)
+k_vorticity_a_coop(const float4* __restrict__ P, const float4* __restrict__ VS,
+                   const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cstart,
+                   const int32_t* __restrict__ cend, float4* __restrict__ VX,
+                   float4* __restrict__ OM, float4* __restrict__ Q, uint32_t n, CP cp) {
+    const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= n) return;
+    const auto& c = cp.at(i);
+    const float3 pi = xyz(P[i]);
+    const float3 vi = xyz(VS[i]);
+    float3 acc = make_float3(0.0f, 0.0f, 0.0f), w = make_float3(0.0f, 0.0f, 0.0f);
+    float tw = 0.0f;
+    float3 tv = make_float3(0.0f, 0.0f, 0.0f), tc = make_float3(0.0f, 0.0f, 0.0f);
+    bool tgrad = false;
+    coop_visit(i, skeys[i], c, cstart, cend, P, pi,
+               [&](uint32_t j, float3 d, float r2) {
+                   const float len = fsqrt(r2);
+                   tv = sub3(xyz(__ldg(VS + j)), vi);  // vorticity.glsl:50
+                   tw = w_poly6(c, len);
+                   tgrad = len != 0.0f;
+                   if (tgrad) tc = cross3(tv, scale3(d, grad_scale(c.kg, c.h, len)));  // :55
+                   return true;
+               },
+               [&](int src) {
+                   acc = fma3(shf(tw, src), shf3(tv, src), acc);  // :52-54
+                   const bool g = __shfl_sync(kFull, tgrad, src);
+                   const float3 cv = shf3(tc, src);
+                   if (g) w = add3(w, cv);  // :55
+               });
+    if ((threadIdx.x & 31u) == 0u) {
+        const float3 vx = fma3(c.cx, acc, vi);  // :58
+        VX[i] = make_float4(vx.x, vx.y, vx.z, 0.0f);
+        OM[i] = make_float4(w.x, w.y, w.z, 0.0f);
+        Q[i] = make_float4(pi.x, pi.y, pi.z, fsqrt(dot3(w, w)));  // :60
+    }
+}
+
+template <class CP>
+__global__ void __launch_bounds__(kBlock)
+k_vorticity_b_coop(const float4* __restrict__ Q, const float4* __restrict__ VX,
+                   const float4* __restrict__ OM, const uint32_t* __restrict__ skeys,
+                   const uint32_t* __restrict__ perm, const int32_t* __restrict__ cstart,
+                   const int32_t* __restrict__ cend, float4* __restrict__ v,
+                   float4* __restrict__ eta_out, uint32_t n, CP cp) {
+    const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= n) return;
+    const auto& c = cp.at(i);
+    const float3 pi = xyz(Q[i]);
+    float3 eta = make_float3(0.0f, 0.0f, 0.0f);
+    float tq = 0.0f;
+    float3 tg = make_float3(0.0f, 0.0f, 0.0f);
+    coop_visit(i, skeys[i], c, cstart, cend, Q, pi,
+               [&](uint32_t j, float3 d, float r2) {
+                   const float len = fsqrt(r2);
+                   if (len == 0.0f) return false;
+                   tq = __ldg(Q + j).w;
+                   tg = scale3(d, grad_scale(c.kg, c.h, len));
+                   return true;
+               },
+               [&](int src) { eta = fma3(shf(tq, src), shf3(tg, src), eta); });  // vorticity.glsl:72
+    if ((threadIdx.x & 31u) == 0u) {
+        if (eta_out) eta_out[i] = make_float4(eta.x, eta.y, eta.z, 0.0f);
+        const float l = fsqrt(dot3(eta, eta));  // :76
+        if (l > 0.0f) eta = make_float3(fdiv(eta.x, l), fdiv(eta.y, l), fdiv(eta.z, l));  // :77-78
+        const float3 vf = fma3(c.dteps, cross3(eta, xyz(OM[i])), xyz(VX[i]));  // :82
+        v[perm[i]] = make_float4(vf.x, vf.y, vf.z, 0.0f);                     // :85
+    }
+}
+
+// Grid of warps, one per particle.
+inline unsigned coop_grid(uint32_t n) { return (unsigned)(((size_t)n * 32 + kBlock - 1) / kBlock); }
+
 // update.glsl:16-28: v = (x* - x_old) / dt, x = x*, scattered back to id order.
 // VS receives the committed velocity in sorted order; when `v_out` is set the
 // velocity is also stored in id order (vorticity confinement disabled).
@@ -669,6 +874,10 @@ template <class CP>
 void launch_lambda_build(SweepCfg sw, cudaStream_t st, const float4* XP, const uint32_t* skeys,
                          const int32_t* cstart, const int32_t* cend, float4* L, float4* aux,
                          NbrLists nl, PairLists pw, ScanPos sx, uint32_t n, CP cp) {
+    if (sw.mode == kCoop) {
+        k_lambda_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(XP, skeys, cstart, cend, L, aux, n, cp);
+        return;
+    }
     PBF_SWEEP_LAUNCH(k_lambda_build, XP, skeys, cstart, cend, L, aux, nl, pw, sx, n, cp);
 }
 template <class CP>
@@ -676,6 +885,10 @@ void launch_lambda(SweepCfg sw, cudaStream_t st, const float4* P, const float4* 
                    const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* L,
                    float4* aux, NbrLists nl, PairLists pw, ScanPos sx, int dmax_slot, uint32_t n,
                    CP cp) {
+    if (sw.mode == kCoop) {
+        k_lambda_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(P, skeys, cstart, cend, L, aux, n, cp);
+        return;
+    }
     PBF_SWEEP_LAUNCH(k_lambda, P, XP, skeys, cstart, cend, L, aux, nl, pw, sx, dmax_slot, n, cp);
 }
 template <class CP>
@@ -683,6 +896,10 @@ void launch_delta_p(SweepCfg sw, cudaStream_t st, const float4* L, const float4*
                     const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* Pn,
                     NbrLists nl, PairLists pr, ScanPos sx, ScanPos sx_out, int dmax_slot,
                     int out_slot, uint32_t n, CP cp, uint32_t* status) {
+    if (sw.mode == kCoop) {
+        k_delta_p_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(L, skeys, cstart, cend, Pn, n, cp, status);
+        return;
+    }
     PBF_SWEEP_LAUNCH(k_delta_p, L, XP, skeys, cstart, cend, Pn, nl, pr, sx, sx_out, dmax_slot,
                      out_slot, n, cp, status);
 }
@@ -696,6 +913,11 @@ void launch_vorticity_a(SweepCfg sw, cudaStream_t st, const float4* P, const flo
                         const float4* VS, const uint32_t* skeys, const int32_t* cstart,
                         const int32_t* cend, float4* VX, float4* OM, float4* Q, NbrLists nl,
                         PairLists pw, ScanPos sx, int dmax_slot, uint32_t n, CP cp) {
+    if (sw.mode == kCoop) {
+        k_vorticity_a_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(P, VS, skeys, cstart, cend, VX, OM, Q,
+                                                               n, cp);
+        return;
+    }
     PBF_SWEEP_LAUNCH(k_vorticity_a, P, XP, VS, skeys, cstart, cend, VX, OM, Q, nl, pw, sx, dmax_slot,
                      n, cp);
 }
@@ -705,6 +927,11 @@ void launch_vorticity_b(SweepCfg sw, cudaStream_t st, const float4* Q, const flo
                         const uint32_t* perm, const int32_t* cstart, const int32_t* cend,
                         float4* v, float4* eta_out, NbrLists nl, PairLists pr, ScanPos sx,
                         int dmax_slot, uint32_t n, CP cp) {
+    if (sw.mode == kCoop) {
+        k_vorticity_b_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(Q, VX, OM, skeys, perm, cstart, cend, v,
+                                                               eta_out, n, cp);
+        return;
+    }
     PBF_SWEEP_LAUNCH(k_vorticity_b, Q, XP, VX, OM, skeys, perm, cstart, cend, v, eta_out, nl, pr, sx,
                      dmax_slot, n, cp);
 }

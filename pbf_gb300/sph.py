@@ -180,7 +180,7 @@ class SPH:
         if block_size is not None:
             t.block_size = int(block_size)
         if sweep_mode is not None:
-            t.sweep_mode = {"direct": 0, "masked": 1}.get(sweep_mode, sweep_mode)
+            t.sweep_mode = {"direct": 0, "masked": 1, "coop": 2}.get(sweep_mode, sweep_mode)
         if pair_list_capacity is not None:
             t.pair_list_capacity = int(pair_list_capacity)
         check(self._lib.pbf_set_tuning(self._h, C.byref(t)), self._h)

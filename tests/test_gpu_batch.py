@@ -51,7 +51,7 @@ def test_batch_scene_params_and_tuning(gpu):
     p = b.scene_params(2)
     p.xsph_viscosity_c = 0.03
     b.set_scene_params(2, p)
-    b.set_tuning(use_neighbour_lists=False)
+    b.set_tuning(use_neighbour_lists=False, sweep_mode="coop")
     b.step(4)
     bx, bv = b.get_state()
     # the same sequence on scene 2 alone

@@ -237,7 +237,9 @@ def test_set_params_rejects_grid_change(gpu):
                                     dict(pair_list_capacity=20, use_neighbour_lists=False),
                                     dict(pair_list_capacity=33, block_size=64),
                                     dict(pair_list_capacity=4096, use_neighbour_lists=True),
-                                    dict(pair_list_capacity=8, use_neighbour_lists=True, skin_h=0.3)])
+                                    dict(pair_list_capacity=8, use_neighbour_lists=True, skin_h=0.3),
+                                    dict(sweep_mode="coop"),
+                                    dict(sweep_mode="coop", use_neighbour_lists=True)])
 def test_tuning_never_changes_results(gpu, oracle_mod, tuning):
     """Neighbour lists, their capacity and skin, the sweep mode and the pair
     lists (capacities 1, 8 and 20 overflow often: the scanning sweep then
@@ -295,7 +297,7 @@ def test_block_size_and_autotune_never_change_results(gpu, oracle_mod):
     with pytest.raises(pg.PbfError):
         g.set_tuning(block_size=48)
     with pytest.raises(pg.PbfError):
-        g.set_tuning(sweep_mode=2)
+        g.set_tuning(sweep_mode=3)
 
 
 @pytest.mark.parametrize("after", [0, 1, 5, 12, 16])
