@@ -202,7 +202,8 @@ typedef struct pbf_tuning {
                                      testing 32 candidates at once and computing their
                                      pair terms in parallel, folded in the same order
                                      (for scenes too small to fill the GPU with a
-                                     thread per particle, and clumped states) */
+                                     thread per particle, and clumped states; the
+                                     default below 32,768 particles per handle) */
     uint32_t pair_list_capacity;  /* with PBF_SWEEP_MASKED and > 0: each lambda sweep
                                      records every particle's candidates within h (in
                                      visit order, up to this many), evaluates its own

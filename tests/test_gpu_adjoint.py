@@ -144,7 +144,7 @@ def test_adjoint_independent_of_tuning(gpu, tuning):
     u[:, 3] = 0
     ref = gpu_grads(p, x4, v4, S, w, u)
     sim = pg.SPH(n, tuple(p.grid), p)
-    sim.set_tuning(**tuning)
+    sim.set_tuning(**{"sweep_mode": "masked", **tuning})
     sim.set_state(x4, v4)
     sim.forward_record(S, 2)
     dx0, dv0, g = sim.backward(w, u)

@@ -244,10 +244,12 @@ def test_tuning_never_changes_results(gpu, oracle_mod, tuning):
     """Neighbour lists, their capacity and skin, the sweep mode and the pair
     lists (capacities 1, 8 and 20 overflow often: the scanning sweep then
     finds the entries past the capacity with a second scan, and the replaying
-    sweep falls back to a scan) are performance knobs only."""
+    sweep falls back to a scan) are performance knobs only.  (A scene this
+    small defaults to the cooperative sweeps; the one-thread modes are set
+    explicitly unless the case names one.)"""
     sc = scenes.plain_16k()
     g = pg.SPH(sc.n, tuple(sc.params.grid), sc.params)
-    g.set_tuning(**tuning)
+    g.set_tuning(**{"sweep_mode": "masked", **tuning})
     g.set_state(sc.x4, sc.v4)
     g.step(30)
     o = run_oracle(oracle_mod, sc.params, sc.x4, sc.v4, 30)
@@ -264,7 +266,7 @@ def test_lists_exact_in_a_calm_scene(gpu, oracle_mod):
     p = sc.params.copy()
     p.epsilon = 5.0
     g = pg.SPH(sc.n, tuple(p.grid), p)
-    g.set_tuning(use_neighbour_lists=True, skin_h=0.15)
+    g.set_tuning(use_neighbour_lists=True, skin_h=0.15, sweep_mode="masked")
     g.set_state(sc.x4, sc.v4)
     g.step(60)
     o = run_oracle(oracle_mod, p, sc.x4, sc.v4, 60)
@@ -280,7 +282,7 @@ def test_block_size_and_autotune_never_change_results(gpu, oracle_mod):
     ox, ov = o.get_state()
     for blk in (32, 128, 256):
         g = pg.SPH(sc.n, tuple(sc.params.grid), sc.params)
-        g.set_tuning(block_size=blk)
+        g.set_tuning(block_size=blk, sweep_mode="masked")
         g.set_state(sc.x4, sc.v4)
         g.step(12)
         assert_bits(g.positions(), ox, f"positions with block {blk}")
