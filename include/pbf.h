@@ -212,6 +212,11 @@ typedef struct pbf_tuning {
                                      the stencil; the same between the two vorticity
                                      passes.  Longer lists fall back to scans.  0 = off;
                                      default 128; PBF_SWEEP_DIRECT records none */
+    uint32_t coop_candidates;     /* with PBF_SWEEP_DIRECT or PBF_SWEEP_MASKED and no skin
+                                     lists: particles whose 27-cell stencil holds more
+                                     than this many candidates are swept by the
+                                     warp-cooperative kernels, the rest a thread each
+                                     (clumped states); 0 = off */
 } pbf_tuning;
 
 enum { PBF_SWEEP_DIRECT = 0, PBF_SWEEP_MASKED = 1, PBF_SWEEP_COOP = 2 };

@@ -71,6 +71,7 @@ class Tuning(C.Structure):
         ("block_size", C.c_uint32),
         ("sweep_mode", C.c_uint32),
         ("pair_list_capacity", C.c_uint32),
+        ("coop_candidates", C.c_uint32),
     ]
 
 

@@ -146,6 +146,14 @@ void apply_tuning(DevConsts& c, const pbf_params& p, const pbf_tuning& t) {
 // win until the fluid clumps).
 constexpr uint32_t kCoopBelow = 32768;
 
+// The autotuner's mixed-sweep candidate: warps for particles with more than
+// 256 stencil candidates (in the dam break's initial lattice, 8 particles
+// per cell, an interior particle has 216).  It wins
+// while the fluid is part clumped (262,144 particles: 2.7 ms per substep
+// against 4.2 cooperative and 5.7 masked) and loses once every particle is
+// over the threshold, so it is not a default.
+constexpr uint32_t kMixedCandidates = 256;
+
 pbf_tuning default_tuning(uint32_t n) {
     pbf_tuning t{};
     t.use_neighbour_lists = 0;
@@ -231,7 +239,7 @@ void free_sim(pbf_sim* s) {
                     s->VS, s->VX, s->OM,    s->Q,    s->keys,   s->skeys, s->perm,
                     s->cstart, s->cend, s->status, s->sort_mem, s->nbr_idx, s->nbr_cnt,
                     s->guard, s->d_consts, s->sid, s->sid_sorted, s->pair_idx, s->pair_cnt,
-                    s->scan_xy, s->scan_z};
+                    s->scan_xy, s->scan_z, s->heavy, s->heavy_list, s->heavy_count};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (s->h_status) cudaFreeHost(s->h_status);
@@ -331,11 +339,21 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
     auto scan_set = [&](int k) { return ScanPos{s->scan_xy + k * half, s->scan_z + k * half}; };
     k_find_cells<<<g, kBlock, 0, st>>>(s->skeys, s->perm, s->xstar, s->XP, n, s->ncells, s->cstart,
                                        s->cend, s->status + 1, s->sid, s->sid_sorted, scan_set(0));
+    // mixed sweeps: flag the particles with more than coop_candidates stencil
+    // candidates; the cooperative kernels sweep those, the others skip them
+    const bool mixed = sb.mode != 3 && !sb.lists && s->tuning.coop_candidates > 0;
+    if (mixed) {
+        cudaError_t me = cudaMemsetAsync(s->heavy_count, 0, sizeof(uint32_t), st);
+        if (me != cudaSuccess) return me;
+        launch_heavy_scan(g, st, s->skeys, s->cstart, s->cend, s->tuning.coop_candidates, n, cps,
+                          s->heavy, s->heavy_list, s->heavy_count);
+    }
     mark(3);
     // 4 solver iterations (calclambda / updatepos).  The first lambda sweep
     // also records the neighbour lists the later sweeps replay.
     const NbrLists nl{s->nbr_idx, s->nbr_cnt, s->guard, s->nbr_cap, n};
-    const PairLists pl{s->pair_idx, s->pair_cnt, s->pair_cap, n};
+    const PairLists pl{s->pair_idx, s->pair_cnt, s->pair_cap, n, mixed ? s->heavy : nullptr,
+                       s->heavy_list, s->heavy_count};
     cudaError_t ge = cudaMemsetAsync(s->guard, 0, sizeof(uint32_t) * (2 + iters), st);
     if (ge != cudaSuccess) return ge;
     const float4* cur = s->XP;
@@ -482,6 +500,7 @@ pbf_status pbf_create_batch(const pbf_params* scene_params, const uint32_t* scen
     ALLOC(VS, n) ALLOC(VX, n) ALLOC(OM, n) ALLOC(Q, n) ALLOC(keys, n) ALLOC(skeys, n)
     ALLOC(perm, n) ALLOC(cstart, s->ncells) ALLOC(cend, s->ncells) ALLOC(status, 2)
     ALLOC(scan_xy, 3 * (((size_t)n + 1) / 2)) ALLOC(scan_z, 3 * (((size_t)n + 1) / 2))
+    ALLOC(heavy, n) ALLOC(heavy_list, n) ALLOC(heavy_count, 1)
     if (num_scenes > 1) {
         ALLOC(d_consts, num_scenes) ALLOC(sid, n) ALLOC(sid_sorted, n)
     }
@@ -648,6 +667,7 @@ pbf_status pbf_autotune(pbf_sim* s, uint32_t trial_substeps, pbf_tuning* best) {
             t.block_size = blk;
             t.sweep_mode = mode;
             t.use_neighbour_lists = 0;
+            t.coop_candidates = 0;
             cand.push_back(t);
             for (float skin : {0.05f, 0.1f, 0.2f}) {
                 t.use_neighbour_lists = 1;
@@ -660,6 +680,11 @@ pbf_status pbf_autotune(pbf_sim* s, uint32_t trial_substeps, pbf_tuning* best) {
         pbf_tuning t = original;  // the warp-cooperative sweeps (block size and lists unused)
         t.sweep_mode = PBF_SWEEP_COOP;
         t.use_neighbour_lists = 0;
+        t.coop_candidates = 0;
+        cand.push_back(t);
+        t.sweep_mode = PBF_SWEEP_MASKED;  // mixed: warps for the particles in dense stencils
+        t.block_size = 256;
+        t.coop_candidates = kMixedCandidates;
         cand.push_back(t);
     }
     float best_ms = 1e30f;

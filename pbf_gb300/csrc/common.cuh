@@ -69,6 +69,9 @@ struct PairLists {
     int32_t* cnt;
     uint32_t cap;
     uint32_t n;
+    const uint8_t* heavy = nullptr;  // mixed sweeps: particles the cooperative kernels take
+    const uint32_t* heavy_list = nullptr;   // their sorted indices
+    const uint32_t* heavy_count = nullptr;  // and how many there are
 };
 
 // Scan copy of a sorted position array, read by the masked stencil scans two

@@ -55,6 +55,11 @@ struct pbf_sim {
     uint32_t* pair_idx = nullptr;
     int32_t* pair_cnt = nullptr;
     uint32_t pair_cap = 0;
+    // mixed sweeps (pbf_tuning::coop_candidates): per-particle flag, the
+    // flagged sorted indices and their count
+    uint8_t* heavy = nullptr;
+    uint32_t* heavy_list = nullptr;
+    uint32_t* heavy_count = nullptr;
     // scan copies (ScanPos) of the predicted positions (set 0) and of the
     // solver iterates (sets 1 and 2, alternating), (n + 1) / 2 pairs per set
     float4* scan_xy = nullptr;

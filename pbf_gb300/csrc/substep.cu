@@ -279,7 +279,7 @@ k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys
                float4* __restrict__ L, float4* __restrict__ aux, NbrLists nl, PairLists pw,
                ScanPos sx, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool live = i < n;
+    const bool live = i < n && !(pw.heavy && pw.heavy[i]);
     float3 pi = make_float3(0.0f, 0.0f, 0.0f);
     if (live) {
         const auto& c = cp.at(i);
@@ -342,7 +342,7 @@ k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
          const int32_t* __restrict__ cend, float4* __restrict__ L, float4* __restrict__ aux,
          NbrLists nl, PairLists pw, ScanPos sx, int dmax_slot, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || (pw.heavy && pw.heavy[i])) return;
     const auto& c = cp.at(i);
     const float3 pi = xyz(P[i]);
     LambdaAcc a{0.0f, 0.0f, make_float3(0.0f, 0.0f, 0.0f)};
@@ -391,7 +391,7 @@ k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
           ScanPos sx, ScanPos sx_out, int dmax_slot, int out_slot, uint32_t n, CP cp,
           uint32_t* status) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool live = i < n;
+    const bool live = i < n && !(pr.heavy && pr.heavy[i]);
     float disp = 0.0f;
     if (live) {
         const auto& c = cp.at(i);
@@ -500,43 +500,58 @@ __device__ __forceinline__ void coop_visit(uint32_t i, uint32_t key, const DevCo
     }
 }
 
+// Particles a cooperative kernel processes: all n (list == nullptr, one warp
+// per particle), or the `*count` entries of `list` (the heavy particles of a
+// mixed sweep), taken by the grid's warps in turn.
+struct CoopWork {
+    const uint32_t* list;
+    const uint32_t* count;
+};
+
+#define PBF_COOP_FOR_EACH(i)                                                                  \
+    const uint32_t warp0_ = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;                     \
+    const uint32_t nwarps_ = (gridDim.x * blockDim.x) >> 5;                                    \
+    const uint32_t total_ = wk.list ? *wk.count : n;                                           \
+    for (uint32_t w_ = warp0_; w_ < total_; w_ += nwarps_)                                     \
+        if (const uint32_t i = wk.list ? wk.list[w_] : w_; true)
+
 template <class CP>
 __global__ void __launch_bounds__(kBlock)
 k_lambda_coop(const float4* __restrict__ P, const uint32_t* __restrict__ skeys,
               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
-              float4* __restrict__ L, float4* __restrict__ aux, uint32_t n, CP cp) {
-    const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (i >= n) return;  // whole warps: n and the lane count agree per warp
-    const auto& c = cp.at(i);
-    const float3 pi = xyz(P[i]);
-    LambdaAcc a{0.0f, 0.0f, make_float3(0.0f, 0.0f, 0.0f)};
-    float tw = 0.0f, tgg = 0.0f;
-    float3 tg = make_float3(0.0f, 0.0f, 0.0f);
-    bool tgrad = false;
-    coop_visit(i, skeys[i], c, cstart, cend, P, pi,
-               [&](uint32_t, float3 d, float r2) {
-                   const float len = fsqrt(r2);
-                   tw = w_poly6(c, len);
-                   tgrad = len != 0.0f;
-                   if (tgrad) {
-                       tg = scale3(d, grad_scale(c.kg_lambda, c.h, len));
-                       tgg = dot3(tg, tg);
-                   }
-                   return true;
-               },
-               [&](int src) {
-                   a.rho = fadd(a.rho, shf(tw, src));  // calclambda.glsl:80-82
-                   const bool g = __shfl_sync(kFull, tgrad, src);
-                   const float gg = shf(tgg, src);
-                   const float3 gv = shf3(tg, src);
-                   if (g) {
-                       a.sumk = fadd(a.sumk, gg);  // :89
-                       a.gi = add3(a.gi, gv);       // :93
-                   }
-               });
-    if ((threadIdx.x & 31u) == 0u) {
-        L[i] = make_float4(pi.x, pi.y, pi.z, lambda_finish(c, a));
-        if (aux) aux[i] = lambda_aux(a);
+              float4* __restrict__ L, float4* __restrict__ aux, uint32_t n, CP cp, CoopWork wk) {
+    PBF_COOP_FOR_EACH(i) {
+        const auto& c = cp.at(i);
+        const float3 pi = xyz(P[i]);
+        LambdaAcc a{0.0f, 0.0f, make_float3(0.0f, 0.0f, 0.0f)};
+        float tw = 0.0f, tgg = 0.0f;
+        float3 tg = make_float3(0.0f, 0.0f, 0.0f);
+        bool tgrad = false;
+        coop_visit(i, skeys[i], c, cstart, cend, P, pi,
+                   [&](uint32_t, float3 d, float r2) {
+                       const float len = fsqrt(r2);
+                       tw = w_poly6(c, len);
+                       tgrad = len != 0.0f;
+                       if (tgrad) {
+                           tg = scale3(d, grad_scale(c.kg_lambda, c.h, len));
+                           tgg = dot3(tg, tg);
+                       }
+                       return true;
+                   },
+                   [&](int src) {
+                       a.rho = fadd(a.rho, shf(tw, src));  // calclambda.glsl:80-82
+                       const bool g = __shfl_sync(kFull, tgrad, src);
+                       const float gg = shf(tgg, src);
+                       const float3 gv = shf3(tg, src);
+                       if (g) {
+                           a.sumk = fadd(a.sumk, gg);  // :89
+                           a.gi = add3(a.gi, gv);       // :93
+                       }
+                   });
+        if ((threadIdx.x & 31u) == 0u) {
+            L[i] = make_float4(pi.x, pi.y, pi.z, lambda_finish(c, a));
+            if (aux) aux[i] = lambda_aux(a);
+        }
     }
 }
 
@@ -544,39 +559,41 @@ template <class CP>
 __global__ void __launch_bounds__(kBlock)
 k_delta_p_coop(const float4* __restrict__ L, const uint32_t* __restrict__ skeys,
                const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
-               float4* __restrict__ Pn, uint32_t n, CP cp, uint32_t* status) {
-    const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (i >= n) return;
-    const auto& c = cp.at(i);
-    const float4 Li = L[i];
-    const float3 pi = xyz(Li);
-    const float li = Li.w;
-    float3 dp = make_float3(0.0f, 0.0f, 0.0f);
-    float tcoef = 0.0f;
-    float3 tg = make_float3(0.0f, 0.0f, 0.0f);
-    coop_visit(i, skeys[i], c, cstart, cend, L, pi,
-               [&](uint32_t j, float3 d, float r2) {
-                   const float len = fsqrt(r2);
-                   if (len == 0.0f) return false;
-                   float sc = fmul(c.scale, w_poly6(c, len));  // updatepos.glsl:57
-                   sc = fmul(sc, sc);                           // :58
-                   sc = fmul(sc, sc);                           // :59
-                   sc = fmul(c.negk, sc);                       // :60
-                   tcoef = fadd(fadd(li, __ldg(L + j).w), sc);  // :65
-                   tg = scale3(d, grad_scale(c.kg, c.h, len));
-                   return true;
-               },
-               [&](int src) { dp = fma3(shf(tcoef, src), shf3(tg, src), dp); });  // :65
-    if ((threadIdx.x & 31u) == 0u) {
-        float3 q = fma3(c.oorho, dp, pi);  // :85
-        q.x = (q.x < c.lo[0]) ? c.lo[0] : q.x;
-        q.x = (c.hi[0] < q.x) ? c.hi[0] : q.x;
-        q.y = (q.y < c.lo[1]) ? c.lo[1] : q.y;
-        q.y = (c.hi[1] < q.y) ? c.hi[1] : q.y;
-        q.z = (q.z < c.lo[2]) ? c.lo[2] : q.z;
-        q.z = (c.hi[2] < q.z) ? c.hi[2] : q.z;
-        if (!finite3(q)) atomicOr(status, kDevNonFinite);
-        Pn[i] = make_float4(q.x, q.y, q.z, 0.0f);
+               float4* __restrict__ Pn, ScanPos sx_out, uint32_t n, CP cp, uint32_t* status,
+               CoopWork wk) {
+    PBF_COOP_FOR_EACH(i) {
+        const auto& c = cp.at(i);
+        const float4 Li = L[i];
+        const float3 pi = xyz(Li);
+        const float li = Li.w;
+        float3 dp = make_float3(0.0f, 0.0f, 0.0f);
+        float tcoef = 0.0f;
+        float3 tg = make_float3(0.0f, 0.0f, 0.0f);
+        coop_visit(i, skeys[i], c, cstart, cend, L, pi,
+                   [&](uint32_t j, float3 d, float r2) {
+                       const float len = fsqrt(r2);
+                       if (len == 0.0f) return false;
+                       float sc = fmul(c.scale, w_poly6(c, len));  // updatepos.glsl:57
+                       sc = fmul(sc, sc);                           // :58
+                       sc = fmul(sc, sc);                           // :59
+                       sc = fmul(c.negk, sc);                       // :60
+                       tcoef = fadd(fadd(li, __ldg(L + j).w), sc);  // :65
+                       tg = scale3(d, grad_scale(c.kg, c.h, len));
+                       return true;
+                   },
+                   [&](int src) { dp = fma3(shf(tcoef, src), shf3(tg, src), dp); });  // :65
+        if ((threadIdx.x & 31u) == 0u) {
+            float3 q = fma3(c.oorho, dp, pi);  // :85
+            q.x = (q.x < c.lo[0]) ? c.lo[0] : q.x;
+            q.x = (c.hi[0] < q.x) ? c.hi[0] : q.x;
+            q.y = (q.y < c.lo[1]) ? c.lo[1] : q.y;
+            q.y = (c.hi[1] < q.y) ? c.hi[1] : q.y;
+            q.z = (q.z < c.lo[2]) ? c.lo[2] : q.z;
+            q.z = (c.hi[2] < q.z) ? c.hi[2] : q.z;
+            if (!finite3(q)) atomicOr(status, kDevNonFinite);
+            Pn[i] = make_float4(q.x, q.y, q.z, 0.0f);
+            if (sx_out.xy) scanpos_store(sx_out, i, q.x, q.y, q.z);
+        }
     }
 }
 
@@ -585,36 +602,37 @@ __global__ void __launch_bounds__(kBlock)
 k_vorticity_a_coop(const float4* __restrict__ P, const float4* __restrict__ VS,
                    const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cstart,
                    const int32_t* __restrict__ cend, float4* __restrict__ VX,
-                   float4* __restrict__ OM, float4* __restrict__ Q, uint32_t n, CP cp) {
-    const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (i >= n) return;
-    const auto& c = cp.at(i);
-    const float3 pi = xyz(P[i]);
-    const float3 vi = xyz(VS[i]);
-    float3 acc = make_float3(0.0f, 0.0f, 0.0f), w = make_float3(0.0f, 0.0f, 0.0f);
-    float tw = 0.0f;
-    float3 tv = make_float3(0.0f, 0.0f, 0.0f), tc = make_float3(0.0f, 0.0f, 0.0f);
-    bool tgrad = false;
-    coop_visit(i, skeys[i], c, cstart, cend, P, pi,
-               [&](uint32_t j, float3 d, float r2) {
-                   const float len = fsqrt(r2);
-                   tv = sub3(xyz(__ldg(VS + j)), vi);  // vorticity.glsl:50
-                   tw = w_poly6(c, len);
-                   tgrad = len != 0.0f;
-                   if (tgrad) tc = cross3(tv, scale3(d, grad_scale(c.kg, c.h, len)));  // :55
-                   return true;
-               },
-               [&](int src) {
-                   acc = fma3(shf(tw, src), shf3(tv, src), acc);  // :52-54
-                   const bool g = __shfl_sync(kFull, tgrad, src);
-                   const float3 cv = shf3(tc, src);
-                   if (g) w = add3(w, cv);  // :55
-               });
-    if ((threadIdx.x & 31u) == 0u) {
-        const float3 vx = fma3(c.cx, acc, vi);  // :58
-        VX[i] = make_float4(vx.x, vx.y, vx.z, 0.0f);
-        OM[i] = make_float4(w.x, w.y, w.z, 0.0f);
-        Q[i] = make_float4(pi.x, pi.y, pi.z, fsqrt(dot3(w, w)));  // :60
+                   float4* __restrict__ OM, float4* __restrict__ Q, uint32_t n, CP cp,
+                   CoopWork wk) {
+    PBF_COOP_FOR_EACH(i) {
+        const auto& c = cp.at(i);
+        const float3 pi = xyz(P[i]);
+        const float3 vi = xyz(VS[i]);
+        float3 acc = make_float3(0.0f, 0.0f, 0.0f), w = make_float3(0.0f, 0.0f, 0.0f);
+        float tw = 0.0f;
+        float3 tv = make_float3(0.0f, 0.0f, 0.0f), tc = make_float3(0.0f, 0.0f, 0.0f);
+        bool tgrad = false;
+        coop_visit(i, skeys[i], c, cstart, cend, P, pi,
+                   [&](uint32_t j, float3 d, float r2) {
+                       const float len = fsqrt(r2);
+                       tv = sub3(xyz(__ldg(VS + j)), vi);  // vorticity.glsl:50
+                       tw = w_poly6(c, len);
+                       tgrad = len != 0.0f;
+                       if (tgrad) tc = cross3(tv, scale3(d, grad_scale(c.kg, c.h, len)));  // :55
+                       return true;
+                   },
+                   [&](int src) {
+                       acc = fma3(shf(tw, src), shf3(tv, src), acc);  // :52-54
+                       const bool g = __shfl_sync(kFull, tgrad, src);
+                       const float3 cv = shf3(tc, src);
+                       if (g) w = add3(w, cv);  // :55
+                   });
+        if ((threadIdx.x & 31u) == 0u) {
+            const float3 vx = fma3(c.cx, acc, vi);  // :58
+            VX[i] = make_float4(vx.x, vx.y, vx.z, 0.0f);
+            OM[i] = make_float4(w.x, w.y, w.z, 0.0f);
+            Q[i] = make_float4(pi.x, pi.y, pi.z, fsqrt(dot3(w, w)));  // :60
+        }
     }
 }
 
@@ -624,31 +642,76 @@ k_vorticity_b_coop(const float4* __restrict__ Q, const float4* __restrict__ VX,
                    const float4* __restrict__ OM, const uint32_t* __restrict__ skeys,
                    const uint32_t* __restrict__ perm, const int32_t* __restrict__ cstart,
                    const int32_t* __restrict__ cend, float4* __restrict__ v,
-                   float4* __restrict__ eta_out, uint32_t n, CP cp) {
-    const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (i >= n) return;
-    const auto& c = cp.at(i);
-    const float3 pi = xyz(Q[i]);
-    float3 eta = make_float3(0.0f, 0.0f, 0.0f);
-    float tq = 0.0f;
-    float3 tg = make_float3(0.0f, 0.0f, 0.0f);
-    coop_visit(i, skeys[i], c, cstart, cend, Q, pi,
-               [&](uint32_t j, float3 d, float r2) {
-                   const float len = fsqrt(r2);
-                   if (len == 0.0f) return false;
-                   tq = __ldg(Q + j).w;
-                   tg = scale3(d, grad_scale(c.kg, c.h, len));
-                   return true;
-               },
-               [&](int src) { eta = fma3(shf(tq, src), shf3(tg, src), eta); });  // vorticity.glsl:72
-    if ((threadIdx.x & 31u) == 0u) {
-        if (eta_out) eta_out[i] = make_float4(eta.x, eta.y, eta.z, 0.0f);
-        const float l = fsqrt(dot3(eta, eta));  // :76
-        if (l > 0.0f) eta = make_float3(fdiv(eta.x, l), fdiv(eta.y, l), fdiv(eta.z, l));  // :77-78
-        const float3 vf = fma3(c.dteps, cross3(eta, xyz(OM[i])), xyz(VX[i]));  // :82
-        v[perm[i]] = make_float4(vf.x, vf.y, vf.z, 0.0f);                     // :85
+                   float4* __restrict__ eta_out, uint32_t n, CP cp, CoopWork wk) {
+    PBF_COOP_FOR_EACH(i) {
+        const auto& c = cp.at(i);
+        const float3 pi = xyz(Q[i]);
+        float3 eta = make_float3(0.0f, 0.0f, 0.0f);
+        float tq = 0.0f;
+        float3 tg = make_float3(0.0f, 0.0f, 0.0f);
+        coop_visit(i, skeys[i], c, cstart, cend, Q, pi,
+                   [&](uint32_t j, float3 d, float r2) {
+                       const float len = fsqrt(r2);
+                       if (len == 0.0f) return false;
+                       tq = __ldg(Q + j).w;
+                       tg = scale3(d, grad_scale(c.kg, c.h, len));
+                       return true;
+                   },
+                   [&](int src) { eta = fma3(shf(tq, src), shf3(tg, src), eta); });  // vorticity.glsl:72
+        if ((threadIdx.x & 31u) == 0u) {
+            if (eta_out) eta_out[i] = make_float4(eta.x, eta.y, eta.z, 0.0f);
+            const float l = fsqrt(dot3(eta, eta));  // :76
+            if (l > 0.0f) eta = make_float3(fdiv(eta.x, l), fdiv(eta.y, l), fdiv(eta.z, l));  // :77-78
+            const float3 vf = fma3(c.dteps, cross3(eta, xyz(OM[i])), xyz(VX[i]));  // :82
+            v[perm[i]] = make_float4(vf.x, vf.y, vf.z, 0.0f);                     // :85
+        }
     }
 }
+
+// Mixed sweeps: the heavy particles (more than `threshold` stencil
+// candidates) go to the cooperative kernels, listed once per substep after
+// the cell pass (the set depends on the cell tables only, so every sweep of
+// the substep agrees on it); the one-thread kernels skip them.  A block
+// appends its heavy particles in ascending order (one atomic per block), so
+// consecutive warps of a cooperative launch work on neighbouring particles.
+template <class CP>
+__global__ void __launch_bounds__(kBlock)
+k_heavy_scan(const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cstart,
+             const int32_t* __restrict__ cend, uint32_t threshold, uint32_t n, CP cp,
+             uint8_t* __restrict__ heavy, uint32_t* __restrict__ list, uint32_t* __restrict__ count) {
+    __shared__ uint32_t warp_off[kBlock / 32];
+    __shared__ uint32_t base;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    bool h = false;
+    if (i < n) {
+        Runs r;
+        runs_of(skeys[i], cp.at(i), cstart, cend, r);
+        uint32_t cand = 0;
+#pragma unroll
+        for (int o = 0; o < 9; ++o) cand += (uint32_t)(r.e[o] - r.b[o]);
+        h = cand > threshold;
+        heavy[i] = h ? 1 : 0;
+    }
+    const uint32_t m = __ballot_sync(0xffffffffu, h);
+    if (lane == 0) warp_off[wid] = __popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (uint32_t w = 0; w < blockDim.x / 32; ++w) {
+            const uint32_t c = warp_off[w];
+            warp_off[w] = t;
+            t += c;
+        }
+        base = t ? atomicAdd(count, t) : 0u;
+    }
+    __syncthreads();
+    if (h) list[base + warp_off[wid] + __popc(m & ((1u << lane) - 1u))] = i;
+}
+
+// Grid of the cooperative kernels of a mixed sweep (the heavy list's length is
+// only known on the device): 8 blocks of 8 warps per SM.
+constexpr unsigned kHeavyGrid = 152 * 8;
 
 // Grid of warps, one per particle.
 inline unsigned coop_grid(uint32_t n) { return (unsigned)(((size_t)n * 32 + kBlock - 1) / kBlock); }
@@ -683,7 +746,7 @@ k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
               float4* __restrict__ VX, float4* __restrict__ OM, float4* __restrict__ Q,
               NbrLists nl, PairLists pw, ScanPos sx, int dmax_slot, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || (pw.heavy && pw.heavy[i])) return;
     const auto& c = cp.at(i);
     const float3 pi = xyz(P[i]);
     const float3 vi = xyz(VS[i]);
@@ -741,7 +804,7 @@ k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ XP,
               float4* __restrict__ v, float4* __restrict__ eta_out, NbrLists nl, PairLists pr,
               ScanPos sx, int dmax_slot, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || (pr.heavy && pr.heavy[i])) return;
     const auto& c = cp.at(i);
     const float3 pi = xyz(Q[i]);
     float3 eta = make_float3(0.0f, 0.0f, 0.0f);
@@ -875,10 +938,14 @@ void launch_lambda_build(SweepCfg sw, cudaStream_t st, const float4* XP, const u
                          const int32_t* cstart, const int32_t* cend, float4* L, float4* aux,
                          NbrLists nl, PairLists pw, ScanPos sx, uint32_t n, CP cp) {
     if (sw.mode == kCoop) {
-        k_lambda_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(XP, skeys, cstart, cend, L, aux, n, cp);
+        k_lambda_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(XP, skeys, cstart, cend, L, aux, n, cp,
+                                                           CoopWork{nullptr, nullptr});
         return;
     }
     PBF_SWEEP_LAUNCH(k_lambda_build, XP, skeys, cstart, cend, L, aux, nl, pw, sx, n, cp);
+    if (pw.heavy)
+        k_lambda_coop<CP><<<kHeavyGrid, kBlock, 0, st>>>(XP, skeys, cstart, cend, L, aux, n, cp,
+                                                         CoopWork{pw.heavy_list, pw.heavy_count});
 }
 template <class CP>
 void launch_lambda(SweepCfg sw, cudaStream_t st, const float4* P, const float4* XP,
@@ -886,10 +953,14 @@ void launch_lambda(SweepCfg sw, cudaStream_t st, const float4* P, const float4* 
                    float4* aux, NbrLists nl, PairLists pw, ScanPos sx, int dmax_slot, uint32_t n,
                    CP cp) {
     if (sw.mode == kCoop) {
-        k_lambda_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(P, skeys, cstart, cend, L, aux, n, cp);
+        k_lambda_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(P, skeys, cstart, cend, L, aux, n, cp,
+                                                           CoopWork{nullptr, nullptr});
         return;
     }
     PBF_SWEEP_LAUNCH(k_lambda, P, XP, skeys, cstart, cend, L, aux, nl, pw, sx, dmax_slot, n, cp);
+    if (pw.heavy)
+        k_lambda_coop<CP><<<kHeavyGrid, kBlock, 0, st>>>(P, skeys, cstart, cend, L, aux, n, cp,
+                                                         CoopWork{pw.heavy_list, pw.heavy_count});
 }
 template <class CP>
 void launch_delta_p(SweepCfg sw, cudaStream_t st, const float4* L, const float4* XP,
@@ -897,11 +968,23 @@ void launch_delta_p(SweepCfg sw, cudaStream_t st, const float4* L, const float4*
                     NbrLists nl, PairLists pr, ScanPos sx, ScanPos sx_out, int dmax_slot,
                     int out_slot, uint32_t n, CP cp, uint32_t* status) {
     if (sw.mode == kCoop) {
-        k_delta_p_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(L, skeys, cstart, cend, Pn, n, cp, status);
+        k_delta_p_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(L, skeys, cstart, cend, Pn,
+                                                            ScanPos{nullptr, nullptr}, n, cp, status,
+                                                            CoopWork{nullptr, nullptr});
         return;
     }
     PBF_SWEEP_LAUNCH(k_delta_p, L, XP, skeys, cstart, cend, Pn, nl, pr, sx, sx_out, dmax_slot,
                      out_slot, n, cp, status);
+    if (pr.heavy)
+        k_delta_p_coop<CP><<<kHeavyGrid, kBlock, 0, st>>>(L, skeys, cstart, cend, Pn, sx_out, n, cp,
+                                                          status,
+                                                          CoopWork{pr.heavy_list, pr.heavy_count});
+}
+template <class CP>
+void launch_heavy_scan(unsigned g, cudaStream_t st, const uint32_t* skeys, const int32_t* cstart,
+                       const int32_t* cend, uint32_t threshold, uint32_t n, CP cp, uint8_t* heavy,
+                       uint32_t* list, uint32_t* count) {
+    k_heavy_scan<CP><<<g, kBlock, 0, st>>>(skeys, cstart, cend, threshold, n, cp, heavy, list, count);
 }
 template <class CP>
 void launch_commit(unsigned g, cudaStream_t st, const float4* P, const uint32_t* perm, float4* x,
@@ -915,11 +998,14 @@ void launch_vorticity_a(SweepCfg sw, cudaStream_t st, const float4* P, const flo
                         PairLists pw, ScanPos sx, int dmax_slot, uint32_t n, CP cp) {
     if (sw.mode == kCoop) {
         k_vorticity_a_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(P, VS, skeys, cstart, cend, VX, OM, Q,
-                                                               n, cp);
+                                                               n, cp, CoopWork{nullptr, nullptr});
         return;
     }
     PBF_SWEEP_LAUNCH(k_vorticity_a, P, XP, VS, skeys, cstart, cend, VX, OM, Q, nl, pw, sx, dmax_slot,
                      n, cp);
+    if (pw.heavy)
+        k_vorticity_a_coop<CP><<<kHeavyGrid, kBlock, 0, st>>>(
+            P, VS, skeys, cstart, cend, VX, OM, Q, n, cp, CoopWork{pw.heavy_list, pw.heavy_count});
 }
 template <class CP>
 void launch_vorticity_b(SweepCfg sw, cudaStream_t st, const float4* Q, const float4* XP,
@@ -929,11 +1015,15 @@ void launch_vorticity_b(SweepCfg sw, cudaStream_t st, const float4* Q, const flo
                         int dmax_slot, uint32_t n, CP cp) {
     if (sw.mode == kCoop) {
         k_vorticity_b_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(Q, VX, OM, skeys, perm, cstart, cend, v,
-                                                               eta_out, n, cp);
+                                                               eta_out, n, cp, CoopWork{nullptr, nullptr});
         return;
     }
     PBF_SWEEP_LAUNCH(k_vorticity_b, Q, XP, VX, OM, skeys, perm, cstart, cend, v, eta_out, nl, pr, sx,
                      dmax_slot, n, cp);
+    if (pr.heavy)
+        k_vorticity_b_coop<CP><<<kHeavyGrid, kBlock, 0, st>>>(
+            Q, VX, OM, skeys, perm, cstart, cend, v, eta_out, n, cp,
+            CoopWork{pr.heavy_list, pr.heavy_count});
 }
 template <class CP>
 void launch_diagnostics(unsigned g, cudaStream_t st, const float4* P, const float4* v,
@@ -957,6 +1047,9 @@ void launch_diagnostics(unsigned g, cudaStream_t st, const float4* P, const floa
                                      const uint32_t*, const int32_t*, const int32_t*, float4*,  \
                                      NbrLists, PairLists, ScanPos, ScanPos, int, int, uint32_t, \
                                      CP, uint32_t*);                                            \
+    template void launch_heavy_scan<CP>(unsigned, cudaStream_t, const uint32_t*, const int32_t*,  \
+                                        const int32_t*, uint32_t, uint32_t, CP, uint8_t*,          \
+                                        uint32_t*, uint32_t*);                                     \
     template void launch_commit<CP>(unsigned, cudaStream_t, const float4*, const uint32_t*,     \
                                     float4*, float4*, float4*, uint32_t, CP);                   \
     template void launch_vorticity_a<CP>(SweepCfg, cudaStream_t, const float4*, const float4*,  \

@@ -50,6 +50,10 @@ void launch_delta_p(SweepCfg sw, cudaStream_t st, const float4* L, const float4*
                     NbrLists nl, PairLists pr, ScanPos sx, ScanPos sx_out, int dmax_slot,
                     int out_slot, uint32_t n, CP cp, uint32_t* status);
 template <class CP>
+void launch_heavy_scan(unsigned g, cudaStream_t st, const uint32_t* skeys, const int32_t* cstart,
+                       const int32_t* cend, uint32_t threshold, uint32_t n, CP cp, uint8_t* heavy,
+                       uint32_t* list, uint32_t* count);
+template <class CP>
 void launch_commit(unsigned g, cudaStream_t st, const float4* P, const uint32_t* perm, float4* x,
                    float4* VS, float4* v_out, uint32_t n, CP cp);
 template <class CP>

@@ -169,7 +169,8 @@ class SPH:
         return t
 
     def set_tuning(self, use_neighbour_lists=None, list_capacity=None, skin_h=None,
-                   block_size=None, sweep_mode=None, pair_list_capacity=None) -> None:
+                   block_size=None, sweep_mode=None, pair_list_capacity=None,
+                   coop_candidates=None) -> None:
         t = self.get_tuning()
         if use_neighbour_lists is not None:
             t.use_neighbour_lists = 1 if use_neighbour_lists else 0
@@ -183,6 +184,8 @@ class SPH:
             t.sweep_mode = {"direct": 0, "masked": 1, "coop": 2}.get(sweep_mode, sweep_mode)
         if pair_list_capacity is not None:
             t.pair_list_capacity = int(pair_list_capacity)
+        if coop_candidates is not None:
+            t.coop_candidates = int(coop_candidates)
         check(self._lib.pbf_set_tuning(self._h, C.byref(t)), self._h)
 
     def autotune(self, trial_substeps: int = 10) -> dict:

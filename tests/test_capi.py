@@ -93,3 +93,44 @@ def test_invalid_arguments_rejected_before_device(product_lib):
     p.wall_lo[0] = 20.0
     assert product_lib.pbf_create(C.byref(p), 10, C.byref(h)) == _capi.PBF_ERR_INVALID_ARGUMENT
     assert product_lib.pbf_radix_sort(None, None, None, 5, 8, None) == _capi.PBF_ERR_INVALID_ARGUMENT
+
+
+MIRRORS = {"pbf_params": "_capi.Params", "pbf_tuning": "_capi.Tuning",
+           "pbf_param_grads": "_capi.ParamGrads", "pbf_diagnostics": "_capi.Diagnostics",
+           "pbf_view": "splat.View"}
+
+
+def test_struct_mirrors_match_header(tmp_path):
+    """Every ctypes mirror of an include/pbf.h struct has the header's size
+    and the same field offsets (a C probe compiled against the header prints
+    them)."""
+    import shutil
+    import subprocess
+    from pbf_gb300 import splat
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    mods = {"_capi": _capi, "splat": splat}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "pbf.h"', "int main(void) {"]
+    for cname, py in MIRRORS.items():
+        mod, cls = py.split(".")
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for field, _ in getattr(mods[mod], cls)._fields_:
+            lines.append(f'printf("{cname} {field} %zu\\n", offsetof({cname}, {field}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "probe.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "probe"
+    subprocess.run([cc, "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                               text=True).stdout.splitlines():
+        cname, key, val = line.split()
+        got[(cname, key)] = int(val)
+    for cname, py in MIRRORS.items():
+        mod, cls = py.split(".")
+        st = getattr(mods[mod], cls)
+        assert C.sizeof(st) == got[(cname, "size")], f"{py} size"
+        for field, _ in st._fields_:
+            assert getattr(st, field).offset == got[(cname, field)], f"{py}.{field} offset"

@@ -128,7 +128,7 @@ def test_adjoint_without_vorticity_and_checkpoint_spacing(gpu, oracle_mod):
 @pytest.mark.parametrize("tuning", [dict(pair_list_capacity=0), dict(pair_list_capacity=3),
                                     dict(sweep_mode="direct", pair_list_capacity=0),
                                     dict(use_neighbour_lists=True, skin_h=0.2),
-                                    dict(sweep_mode="coop")])
+                                    dict(sweep_mode="coop"), dict(coop_candidates=100)])
 def test_adjoint_independent_of_tuning(gpu, tuning):
     """The reverse sweeps scan once per position set into the pair-list
     buffer and replay it; without pair lists, or with lists that overflow

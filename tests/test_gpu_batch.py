@@ -42,6 +42,24 @@ def test_batch_matches_single_handles_and_oracle(gpu, oracle_mod):
         assert_bits(bv[sl], rv, f"scene {k} velocities vs oracle")
 
 
+@pytest.mark.parametrize("threshold", [1, 40, 120])
+def test_batch_mixed_sweeps(gpu, threshold):
+    """Mixed sweeps over a batch: the heavy list spans scenes (each particle
+    keeps its own scene's constants in the cooperative kernels), and the
+    result is the same bits as the one-thread sweeps."""
+    sc = small_batch(5, seed=21)
+    x4, v4 = scenes.concat_state(sc)
+    runs = []
+    for thr in (0, threshold):
+        b = pg.SPHBatch([s.params for s in sc], [s.n for s in sc])
+        b.set_tuning(sweep_mode="masked", coop_candidates=thr)
+        b.set_state(x4, v4)
+        b.step(10)
+        runs.append(b.get_state())
+    assert_bits(runs[1][0], runs[0][0], f"positions, mixed threshold {threshold}")
+    assert_bits(runs[1][1], runs[0][1], f"velocities, mixed threshold {threshold}")
+
+
 def test_batch_scene_params_and_tuning(gpu):
     sc = small_batch(4, seed=11)
     b = pg.SPHBatch([s.params for s in sc], [s.n for s in sc])

@@ -239,12 +239,20 @@ def test_set_params_rejects_grid_change(gpu):
                                     dict(pair_list_capacity=4096, use_neighbour_lists=True),
                                     dict(pair_list_capacity=8, use_neighbour_lists=True, skin_h=0.3),
                                     dict(sweep_mode="coop"),
-                                    dict(sweep_mode="coop", use_neighbour_lists=True)])
+                                    dict(sweep_mode="coop", use_neighbour_lists=True),
+                                    dict(coop_candidates=1),
+                                    dict(coop_candidates=100),
+                                    dict(coop_candidates=200, pair_list_capacity=20),
+                                    dict(coop_candidates=150, sweep_mode="direct"),
+                                    dict(coop_candidates=100, pair_list_capacity=0, block_size=64),
+                                    dict(coop_candidates=100, use_neighbour_lists=True)])
 def test_tuning_never_changes_results(gpu, oracle_mod, tuning):
     """Neighbour lists, their capacity and skin, the sweep mode and the pair
     lists (capacities 1, 8 and 20 overflow often: the scanning sweep then
     finds the entries past the capacity with a second scan, and the replaying
-    sweep falls back to a scan) are performance knobs only.  (A scene this
+    sweep falls back to a scan) and the mixed sweeps (the particles with more
+    than coop_candidates stencil candidates swept by warps, the rest by
+    threads; ignored with skin lists) are performance knobs only.  (A scene this
     small defaults to the cooperative sweeps; the one-thread modes are set
     explicitly unless the case names one.)"""
     sc = scenes.plain_16k()
