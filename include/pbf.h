@@ -217,13 +217,36 @@ typedef struct pbf_tuning {
                                      than this many candidates are swept by the
                                      warp-cooperative kernels, the rest a thread each
                                      (clumped states); 0 = off */
+    uint32_t auto_period;         /* PBF_SWEEP_AUTO: substeps before the first trial and
+                                     between trials while the choice keeps changing
+                                     (doubling up to 256 substeps while it holds);
+                                     0 = 32 */
 } pbf_tuning;
 
-enum { PBF_SWEEP_DIRECT = 0, PBF_SWEEP_MASKED = 1, PBF_SWEEP_COOP = 2 };
+/* PBF_SWEEP_AUTO (default): the solver sweeps (lambda + delta-p) and the two
+ * vorticity passes each run one of the PBF_PASS_* configurations.  A trial
+ * steps one real substep under each candidate configuration with stage
+ * events, and the handle keeps the fastest solver and vorticity
+ * configurations.  Every configuration gives the same bits, so trials change
+ * no result; skin lists are not used.  Handles start with PBF_PASS_COOP below
+ * 32,768 particles and PBF_PASS_MASKED from there. */
+enum { PBF_SWEEP_DIRECT = 0, PBF_SWEEP_MASKED = 1, PBF_SWEEP_COOP = 2, PBF_SWEEP_AUTO = 3 };
+enum {
+    PBF_PASS_MASKED = 0,      /* masked scans (with pair lists when pair_list_capacity > 0) */
+    PBF_PASS_DIRECT = 1,      /* direct stencil loops */
+    PBF_PASS_COOP = 2,        /* warp-cooperative sweeps */
+    PBF_PASS_DIRECT_COOP = 3  /* direct first sweep (lambda, vorticity a), cooperative second
+                                 (delta-p, vorticity b) */
+};
 
 /* No reference counterpart (the reference has no tuning surface). */
 pbf_status pbf_set_tuning(pbf_sim* sim, const pbf_tuning* tuning);
 pbf_status pbf_get_tuning(const pbf_sim* sim, pbf_tuning* out);
+/* The PBF_PASS_* configurations the next substep runs for the solver sweeps
+ * (out[0]) and the vorticity passes (out[1]), and the number of
+ * PBF_SWEEP_AUTO trials since the last state upload or tuning change
+ * (out[2]).  No reference counterpart. */
+pbf_status pbf_get_sweep_choice(const pbf_sim* sim, uint32_t out[3]);
 
 /* Autotuner: times `trial_substeps` substeps from the current state under
  * each candidate tuning (sweep block size 128 / 256; direct or masked

@@ -72,6 +72,7 @@ class Tuning(C.Structure):
         ("sweep_mode", C.c_uint32),
         ("pair_list_capacity", C.c_uint32),
         ("coop_candidates", C.c_uint32),
+        ("auto_period", C.c_uint32),
     ]
 
 
@@ -125,6 +126,7 @@ SIGNATURES = {
     "pbf_synchronize": (C.c_int, [_P]),
     "pbf_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
     "pbf_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+    "pbf_get_sweep_choice": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
     "pbf_autotune": (C.c_int, [_P, C.c_uint32, C.POINTER(Tuning)]),
     "pbf_device_status": (C.c_int, [_P, _U32P]),
     "pbf_enable_timing": (C.c_int, [_P, C.c_int]),

@@ -160,9 +160,67 @@ pbf_tuning default_tuning(uint32_t n) {
     t.list_capacity = 128;
     t.skin_h = 0.15f;
     t.block_size = 256;
-    t.sweep_mode = n < kCoopBelow ? PBF_SWEEP_COOP : PBF_SWEEP_MASKED;
+    t.sweep_mode = PBF_SWEEP_AUTO;
     t.pair_list_capacity = 128;
+    (void)n;
     return t;
+}
+
+// PBF_SWEEP_AUTO: substeps before the first trial and between trials while
+// the choice changes; the period doubles up to kAutoPeriodMax while it holds.
+// A candidate replaces the current configuration only if it was at least 3%
+// faster in the trial (the state drifts between the trial's substeps).
+constexpr uint32_t kAutoPeriod = 32;
+constexpr uint32_t kAutoPeriodMax = 256;
+constexpr double kAutoMargin = 0.97;
+// The all-cooperative candidate is tried below this many particles only: a
+// warp per particle costs ~3x the instructions and, on a GPU that a thread per
+// particle already fills, a trial substep under it costs several substeps.
+constexpr uint32_t kCoopTrialBelow = 262144;
+
+// Chooses the starting configuration and the candidates, and restarts the
+// trial schedule (a new state or tuning).
+void reset_sweep_choice(pbf_sim* s) {
+    const uint32_t m = s->tuning.sweep_mode;
+    uint32_t pass = m == PBF_SWEEP_DIRECT ? PBF_PASS_DIRECT
+                    : m == PBF_SWEEP_COOP ? PBF_PASS_COOP
+                                          : PBF_PASS_MASKED;
+    if (m == PBF_SWEEP_AUTO) pass = s->n < kCoopBelow ? PBF_PASS_COOP : PBF_PASS_MASKED;
+    s->pass_solver = s->pass_vort = pass;
+    s->auto_period = s->tuning.auto_period ? s->tuning.auto_period : kAutoPeriod;
+    s->auto_count = 0;
+    s->auto_next = s->auto_period;
+    s->auto_trial = -1;
+    s->auto_trials = 0;
+    s->auto_cands = {PBF_PASS_MASKED, PBF_PASS_DIRECT, PBF_PASS_DIRECT_COOP};
+    if (s->n < kCoopTrialBelow) s->auto_cands.push_back(PBF_PASS_COOP);
+}
+
+// SweepCfg modes (0 direct, 1 masked, 2 masked + pair lists, 3 cooperative)
+// of a pass's first and second sweep.
+struct PassModes {
+    int first, second;
+};
+PassModes modes_of(const pbf_sim* s, uint32_t pass) {
+    switch (pass) {
+        case PBF_PASS_DIRECT: return {0, 0};
+        case PBF_PASS_COOP: return {3, 3};
+        case PBF_PASS_DIRECT_COOP: return {0, 3};
+        default: {
+            const int masked = s->pair_cap ? 2 : 1;
+            return {masked, masked};
+        }
+    }
+}
+bool skin_lists_on(const pbf_sim* s) {
+    return s->tuning.use_neighbour_lists != 0 && s->tuning.sweep_mode != PBF_SWEEP_AUTO;
+}
+// Mixed sweeps run when asked for and some sweep runs a thread per particle.
+bool mixed_on(const pbf_sim* s) {
+    if (s->tuning.coop_candidates == 0 || skin_lists_on(s)) return false;
+    const PassModes a = modes_of(s, s->pass_solver), b = modes_of(s, s->pass_vort);
+    const bool vort = s->params.vorticity_confinement != 0;
+    return a.first != 3 || a.second != 3 || (vort && (b.first != 3 || b.second != 3));
 }
 
 // Host-side fault injection (pbf_debug_fail_allocation): when armed, the
@@ -233,8 +291,12 @@ void free_sim(pbf_sim* s) {
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
     free_tape(s);
-    if (s->exec) cudaGraphExecDestroy(s->exec);
-    if (s->graph) cudaGraphDestroy(s->graph);
+    for (int k = 0; k < 16; ++k) {
+        if (s->execs[k]) cudaGraphExecDestroy(s->execs[k]);
+        if (s->graphs[k]) cudaGraphDestroy(s->graphs[k]);
+    }
+    for (cudaEvent_t e : s->trial_ev)
+        if (e) cudaEventDestroy(e);
     void* bufs[] = {s->x,  s->v,  s->xstar, s->XP,   s->Pa,     s->Pb,   s->L,
                     s->VS, s->VX, s->OM,    s->Q,    s->keys,   s->skeys, s->perm,
                     s->cstart, s->cend, s->status, s->sort_mem, s->nbr_idx, s->nbr_cnt,
@@ -255,14 +317,94 @@ void free_sim(pbf_sim* s) {
 // Kernel launches per substep (the sort's launches plus one per stage).
 uint32_t kernels_per_substep(const pbf_sim* s) {
     const uint32_t passes = (s->numbits + 7) / 8;
-    return 1u /*predict*/ + 1u /*unmark*/ + 2u + passes /*sort*/ + 1u /*cells*/ +
-           2u * s->params.num_solver_iterations + 1u /*commit*/ +
-           (s->params.vorticity_confinement ? 2u : 0u);
+    const uint32_t iters = s->params.num_solver_iterations;
+    const bool vort = s->params.vorticity_confinement != 0;
+    uint32_t k = 1u /*predict*/ + 1u /*unmark*/ + 2u + passes /*sort*/ + 1u /*cells*/ +
+                 2u * iters + 1u /*commit*/ + (vort ? 2u : 0u);
+    if (mixed_on(s)) {  // the flag pass and a cooperative launch after each one-thread sweep
+        const PassModes a = modes_of(s, s->pass_solver), b = modes_of(s, s->pass_vort);
+        k += 1u + iters * ((a.first != 3) + (a.second != 3)) +
+             (vort ? (uint32_t)((b.first != 3) + (b.second != 3)) : 0u);
+    }
+    return k;
 }
 
 // One eager substep with stage events; accumulates the stage sums.
 pbf_status timed_substep(pbf_sim* s);
 
+
+// Launches `count` substeps of the captured graph of the current solver and
+// vorticity configurations (captured on first use).
+pbf_status launch_graph(pbf_sim* s, uint32_t count) {
+    const uint32_t key = s->pass_solver * 4u + s->pass_vort;
+    if (!s->execs[key]) {
+        PBF_CUDA(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = enqueue_substep(s, nullptr);
+        cudaGraph_t g = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
+        if (e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return cuda_fail(s, e, "substep capture");
+        }
+        if (e2 != cudaSuccess) return cuda_fail(s, e2, "cudaStreamEndCapture");
+        s->graphs[key] = g;
+        PBF_CUDA(s, cudaGraphInstantiate(&s->execs[key], g, 0));
+    }
+    for (uint32_t k = 0; k < count; ++k) PBF_CUDA(s, cudaGraphLaunch(s->execs[key], s->stream));
+    return PBF_OK;
+}
+
+// One substep of a PBF_SWEEP_AUTO trial: the next candidate configuration for
+// both passes, eager, with stage events.  After the last candidate, waits for
+// the trial's events and keeps, for the solver sweeps and for the vorticity
+// passes separately, the fastest configuration (a candidate must beat the
+// current one by kAutoMargin).  The period doubles while the choice holds.
+pbf_status trial_substep(pbf_sim* s) {
+    NvtxRange nvtx_("sweep trial substep");
+    const uint32_t iters = s->params.num_solver_iterations;
+    const size_t per = 7 + 2 * (size_t)iters;
+    const size_t nc = s->auto_cands.size();
+    while (s->trial_ev.size() < per * nc) {
+        cudaEvent_t e = nullptr;
+        PBF_CUDA(s, cudaEventCreate(&e));
+        s->trial_ev.push_back(e);
+    }
+    const uint32_t keep_s = s->pass_solver, keep_v = s->pass_vort;
+    const int k = s->auto_trial;
+    s->pass_solver = s->pass_vort = s->auto_cands[k];
+    cudaError_t e = enqueue_substep(s, s->trial_ev.data() + per * k);
+    s->pass_solver = keep_s;
+    s->pass_vort = keep_v;
+    if (e != cudaSuccess) return cuda_fail(s, e, "trial substep launch");
+    if (++s->auto_trial < (int)nc) return PBF_OK;
+    PBF_CUDA(s, cudaEventSynchronize(s->trial_ev[per * nc - 1]));
+    auto span = [&](size_t c, size_t a, size_t b) {
+        float m = 0.0f;
+        cudaEventElapsedTime(&m, s->trial_ev[per * c + a], s->trial_ev[per * c + b]);
+        return (double)m;
+    };
+    auto pick = [&](uint32_t cur, size_t a, size_t b) {
+        size_t best = 0, at_cur = 0;
+        for (size_t c = 0; c < nc; ++c) {
+            if (span(c, a, b) < span(best, a, b)) best = c;
+            if (s->auto_cands[c] == cur) at_cur = c;
+        }
+        return span(best, a, b) < kAutoMargin * span(at_cur, a, b) ? s->auto_cands[best] : cur;
+    };
+    const uint32_t ns = pick(s->pass_solver, 3, 3 + 2 * (size_t)iters);
+    const uint32_t nv = s->params.vorticity_confinement
+                            ? pick(s->pass_vort, 4 + 2 * (size_t)iters, 6 + 2 * (size_t)iters)
+                            : s->pass_vort;
+    const bool changed = ns != s->pass_solver || nv != s->pass_vort;
+    s->pass_solver = ns;
+    s->pass_vort = nv;
+    const uint32_t base = s->tuning.auto_period ? s->tuning.auto_period : kAutoPeriod;
+    s->auto_period = changed ? base : std::min(2 * s->auto_period, std::max(base, kAutoPeriodMax));
+    s->auto_next = s->auto_count + 1 + s->auto_period;  // counted after this substep
+    s->auto_trial = -1;
+    s->auto_trials++;
+    return PBF_OK;
+}
 
 pbf_status timed_substep(pbf_sim* s) {
     NvtxRange nvtx_("timed substep");
@@ -314,11 +456,18 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
     if (!s->nbr_cnt || s->guard_slots < 2 + s->params.num_solver_iterations)
         return cudaErrorInvalidValue;  // ensure_lists() runs before any capture
     const unsigned g = grid_for(n);
-    const SweepCfg sb{s->tuning.block_size ? s->tuning.block_size : (unsigned)kBlock,
-                      s->tuning.sweep_mode == PBF_SWEEP_MASKED ? (s->pair_cap ? 2 : 1)
-                      : s->tuning.sweep_mode == PBF_SWEEP_COOP ? 3
-                                                               : 0,
-                      s->tuning.use_neighbour_lists != 0};
+    const unsigned blk = s->tuning.block_size ? s->tuning.block_size : (unsigned)kBlock;
+    const bool lists = skin_lists_on(s);
+    const PassModes ms = modes_of(s, s->pass_solver), mv = modes_of(s, s->pass_vort);
+    const SweepCfg s_lam{blk, ms.first, lists}, s_dp{blk, ms.second, lists},
+        s_va{blk, mv.first, lists}, s_vb{blk, mv.second, lists};
+    const bool vort = s->params.vorticity_confinement != 0;
+    // delta-p writes the scan copy of its output when a sweep reading that
+    // position set scans through it (masked modes; a pair-list replay falls
+    // back to a scan on overflow)
+    auto scans = [](int m) { return m == 1 || m == 2; };
+    const bool solver_scans = scans(ms.first) || scans(ms.second);
+    const bool vort_scans = vort && (scans(mv.first) || scans(mv.second));
     const uint32_t iters = s->params.num_solver_iterations;
     cudaStream_t st = s->stream;
     auto mark = [&](uint32_t idx) {
@@ -341,7 +490,7 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
                                        s->cend, s->status + 1, s->sid, s->sid_sorted, scan_set(0));
     // mixed sweeps: flag the particles with more than coop_candidates stencil
     // candidates; the cooperative kernels sweep those, the others skip them
-    const bool mixed = sb.mode != 3 && !sb.lists && s->tuning.coop_candidates > 0;
+    const bool mixed = mixed_on(s);
     if (mixed) {
         cudaError_t me = cudaMemsetAsync(s->heavy_count, 0, sizeof(uint32_t), st);
         if (me != cudaSuccess) return me;
@@ -366,16 +515,17 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
         float4* aux = rec ? rec->AUX[it] : nullptr;
         const int in_slot = it == 0 ? -1 : (int)it;  // displacement of `cur` from XP
         if (it == 0)
-            launch_lambda_build(sb, st, s->XP, s->skeys, s->cstart, s->cend, Lk, aux, nl, pl,
+            launch_lambda_build(s_lam, st, s->XP, s->skeys, s->cstart, s->cend, Lk, aux, nl, pl,
                                 scan_set(0), n, cps);
         else
-            launch_lambda(sb, st, cur, s->XP, s->skeys, s->cstart, s->cend, Lk, aux, nl, pl,
+            launch_lambda(s_lam, st, cur, s->XP, s->skeys, s->cstart, s->cend, Lk, aux, nl, pl,
                           scan_set(cur_set), in_slot, n, cps);
         mark(4 + 2 * it);
         // delta-p replays the pair lists the lambda sweep just recorded
-        launch_delta_p(sb, st, Lk, s->XP, s->skeys, s->cstart, s->cend, nxt, nl, pl,
-                       scan_set(cur_set), scan_set(nxt_set), in_slot, (int)it + 1, n, cps,
-                       s->status);
+        const bool write_scan = it + 1 < iters ? solver_scans : vort_scans;
+        launch_delta_p(s_dp, st, Lk, s->XP, s->skeys, s->cstart, s->cend, nxt, nl, pl,
+                       scan_set(cur_set), write_scan ? scan_set(nxt_set) : ScanPos{nullptr, nullptr},
+                       in_slot, (int)it + 1, n, cps, s->status);
         mark(5 + 2 * it);
         cur = nxt;
         cur_set = nxt_set;
@@ -387,7 +537,6 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
         cur = rec->PF;
     }
     // 5 commit (update.glsl) and XSPH + vorticity (vorticity.glsl)
-    const bool vort = s->params.vorticity_confinement != 0;
     const int fin_slot = iters == 0 ? -2 : (int)iters;  // -2: no list was built this substep
     float4* VS = rec ? rec->VS : s->VS;
     float4* OM = rec ? rec->OM : s->OM;
@@ -395,11 +544,11 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
     launch_commit(g, st, cur, s->perm, s->x, VS, vort ? nullptr : s->v, n, cps);
     mark(4 + 2 * iters);
     if (vort)
-        launch_vorticity_a(sb, st, cur, s->XP, VS, s->skeys, s->cstart, s->cend, s->VX, OM, Q, nl,
+        launch_vorticity_a(s_va, st, cur, s->XP, VS, s->skeys, s->cstart, s->cend, s->VX, OM, Q, nl,
                            pl, scan_set(cur_set), fin_slot, n, cps);
     mark(5 + 2 * iters);
     if (vort)
-        launch_vorticity_b(sb, st, Q, s->XP, s->VX, OM, s->skeys, s->perm, s->cstart, s->cend, s->v,
+        launch_vorticity_b(s_vb, st, Q, s->XP, s->VX, OM, s->skeys, s->perm, s->cstart, s->cend, s->v,
                            rec ? rec->ETA : nullptr, nl, pl, scan_set(cur_set), fin_slot, n, cps);
     mark(6 + 2 * iters);
     return cudaGetLastError();
@@ -412,11 +561,12 @@ cudaError_t enqueue_substep(pbf_sim* s, cudaEvent_t* ev, const Recording* rec) {
 }
 
 void invalidate_graph(pbf_sim* s) {
-    if (s->exec) cudaGraphExecDestroy(s->exec);
-    if (s->graph) cudaGraphDestroy(s->graph);
-    s->exec = nullptr;
-    s->graph = nullptr;
-    s->graph_valid = false;
+    for (int k = 0; k < 16; ++k) {
+        if (s->execs[k]) cudaGraphExecDestroy(s->execs[k]);
+        if (s->graphs[k]) cudaGraphDestroy(s->graphs[k]);
+        s->execs[k] = nullptr;
+        s->graphs[k] = nullptr;
+    }
 }
 
 pbf_status check_status(pbf_sim* s) {
@@ -515,6 +665,7 @@ pbf_status pbf_create_batch(const pbf_params* scene_params, const uint32_t* scen
         return st;
     }
     s->stream = s->own_stream;
+    reset_sweep_choice(s);
     s->sort.carve(s->sort_mem, n);
     e = cudaMemsetAsync(s->cstart, 0xFF, sizeof(int32_t) * s->ncells, s->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(s->cend, 0xFF, sizeof(int32_t) * s->ncells, s->stream);
@@ -581,6 +732,7 @@ pbf_status pbf_set_scene_params(pbf_sim* s, uint32_t scene, const pbf_params* p)
                                cudaMemcpyHostToDevice));
     invalidate_graph(s);
     free_tape(s);  // a recorded run is only valid for the parameters it ran with
+    s->auto_trial = -1;  // a running trial's events may not match the new iteration count
     PBF_CUDA(s, ensure_lists(s));
     return PBF_OK;
 }
@@ -614,9 +766,10 @@ pbf_status pbf_set_tuning(pbf_sim* s, const pbf_tuning* t) {
     if (t->pair_list_capacity > 4096)
         return fail(s, PBF_ERR_INVALID_ARGUMENT, "pair_list_capacity must be in [0, 4096]");
     if (t->sweep_mode != PBF_SWEEP_DIRECT && t->sweep_mode != PBF_SWEEP_MASKED &&
-        t->sweep_mode != PBF_SWEEP_COOP)
+        t->sweep_mode != PBF_SWEEP_COOP && t->sweep_mode != PBF_SWEEP_AUTO)
         return fail(s, PBF_ERR_INVALID_ARGUMENT,
-                    "sweep_mode must be PBF_SWEEP_DIRECT, PBF_SWEEP_MASKED or PBF_SWEEP_COOP");
+                    "sweep_mode must be PBF_SWEEP_DIRECT, PBF_SWEEP_MASKED, PBF_SWEEP_COOP or "
+                    "PBF_SWEEP_AUTO");
     DeviceGuard dg(s->device);
     PBF_CUDA(s, cudaStreamSynchronize(s->stream));
     s->tuning = *t;
@@ -627,6 +780,7 @@ pbf_status pbf_set_tuning(pbf_sim* s, const pbf_tuning* t) {
                                cudaMemcpyHostToDevice));
     invalidate_graph(s);
     PBF_CUDA(s, ensure_lists(s));
+    reset_sweep_choice(s);
     return PBF_OK;
 }
 
@@ -760,6 +914,7 @@ pbf_status pbf_set_state(pbf_sim* s, const float* x4, const float* v4, int where
     PBF_CUDA(s, cudaMemcpyAsync(s->x, x4, sizeof(float4) * s->n, k, s->stream));
     PBF_CUDA(s, cudaMemcpyAsync(s->v, v4, sizeof(float4) * s->n, k, s->stream));
     PBF_CUDA(s, cudaStreamSynchronize(s->stream));
+    reset_sweep_choice(s);
     return PBF_OK;
 }
 
@@ -792,22 +947,32 @@ pbf_status pbf_step(pbf_sim* s, uint32_t substeps) {
         }
         return PBF_OK;
     }
-    if (!s->graph_valid) {
-        invalidate_graph(s);
-        PBF_CUDA(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-        cudaError_t e = enqueue_substep(s, nullptr);
-        cudaGraph_t g = nullptr;
-        cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
-        if (e != cudaSuccess) {
-            if (g) cudaGraphDestroy(g);
-            return cuda_fail(s, e, "substep capture");
+    const bool autom = s->tuning.sweep_mode == PBF_SWEEP_AUTO;
+    uint32_t left = substeps;
+    while (left > 0) {
+        if (autom && s->auto_trial < 0 && s->auto_count >= s->auto_next) s->auto_trial = 0;
+        if (autom && s->auto_trial >= 0) {
+            pbf_status r = trial_substep(s);
+            if (r != PBF_OK) return r;
+            --left;
+            ++s->auto_count;
+            continue;
         }
-        if (e2 != cudaSuccess) return cuda_fail(s, e2, "cudaStreamEndCapture");
-        s->graph = g;
-        PBF_CUDA(s, cudaGraphInstantiate(&s->exec, s->graph, 0));
-        s->graph_valid = true;
+        uint32_t run = left;
+        if (autom) run = (uint32_t)std::min<uint64_t>(left, s->auto_next - s->auto_count);
+        pbf_status r = launch_graph(s, run);
+        if (r != PBF_OK) return r;
+        left -= run;
+        s->auto_count += run;
     }
-    for (uint32_t k = 0; k < substeps; ++k) PBF_CUDA(s, cudaGraphLaunch(s->exec, s->stream));
+    return PBF_OK;
+}
+
+pbf_status pbf_get_sweep_choice(const pbf_sim* s, uint32_t out[3]) {
+    if (!s || !out) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "NULL argument");
+    out[0] = s->pass_solver;
+    out[1] = s->pass_vort;
+    out[2] = s->auto_trials;
     return PBF_OK;
 }
 

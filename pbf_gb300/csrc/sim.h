@@ -68,9 +68,21 @@ struct pbf_sim {
     void* sort_mem = nullptr;
     SortWorkspace sort;
 
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    bool graph_valid = false;
+    // PBF_PASS_* configuration of the solver sweeps and the vorticity passes
+    // the next substep runs; one captured graph per pair
+    uint32_t pass_solver = 0, pass_vort = 0;
+    cudaGraph_t graphs[16] = {};
+    cudaGraphExec_t execs[16] = {};
+
+    // PBF_SWEEP_AUTO: substeps since the last reset, substep of the next
+    // trial, current trial period, candidate the running trial steps next
+    // (-1: none), trials so far, the trial's candidates and their events
+    uint64_t auto_count = 0, auto_next = 0;
+    uint32_t auto_period = 0;
+    int auto_trial = -1;
+    uint32_t auto_trials = 0;
+    std::vector<uint32_t> auto_cands;
+    std::vector<cudaEvent_t> trial_ev;  // (7 + 2 * iterations) per candidate
 
     bool timing = false;
     std::vector<cudaEvent_t> ev;  // 7 + 2 * iterations stage boundaries

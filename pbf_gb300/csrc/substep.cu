@@ -439,7 +439,7 @@ k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
         q.z = (c.hi[2] < q.z) ? c.hi[2] : q.z;
         if (!finite3(q)) atomicOr(status, kDevNonFinite);
         Pn[i] = make_float4(q.x, q.y, q.z, 0.0f);
-        if (MODE != kDirect) scanpos_store(sx_out, i, q.x, q.y, q.z);
+        if (sx_out.xy) scanpos_store(sx_out, i, q.x, q.y, q.z);
         if (LISTS) {
             const float3 dd = make_float3(q.x - xi.x, q.y - xi.y, q.z - xi.z);
             disp = sqrtf(dd.x * dd.x + dd.y * dd.y + dd.z * dd.z);

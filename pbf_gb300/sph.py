@@ -170,7 +170,7 @@ class SPH:
 
     def set_tuning(self, use_neighbour_lists=None, list_capacity=None, skin_h=None,
                    block_size=None, sweep_mode=None, pair_list_capacity=None,
-                   coop_candidates=None) -> None:
+                   coop_candidates=None, auto_period=None) -> None:
         t = self.get_tuning()
         if use_neighbour_lists is not None:
             t.use_neighbour_lists = 1 if use_neighbour_lists else 0
@@ -181,12 +181,25 @@ class SPH:
         if block_size is not None:
             t.block_size = int(block_size)
         if sweep_mode is not None:
-            t.sweep_mode = {"direct": 0, "masked": 1, "coop": 2}.get(sweep_mode, sweep_mode)
+            t.sweep_mode = {"direct": 0, "masked": 1, "coop": 2, "auto": 3}.get(sweep_mode, sweep_mode)
         if pair_list_capacity is not None:
             t.pair_list_capacity = int(pair_list_capacity)
         if coop_candidates is not None:
             t.coop_candidates = int(coop_candidates)
+        if auto_period is not None:
+            t.auto_period = int(auto_period)
         check(self._lib.pbf_set_tuning(self._h, C.byref(t)), self._h)
+
+    PASSES = ("masked", "direct", "coop", "direct+coop")
+
+    def sweep_choice(self) -> dict:
+        """The configurations the next substep runs for the solver sweeps and
+        the vorticity passes, and the automatic-mode trials so far
+        (pbf_get_sweep_choice)."""
+        out = (C.c_uint32 * 3)()
+        check(self._lib.pbf_get_sweep_choice(self._h, out), self._h)
+        return {"solver": self.PASSES[out[0]], "vorticity": self.PASSES[out[1]],
+                "trials": int(out[2])}
 
     def autotune(self, trial_substeps: int = 10) -> dict:
         """Picks the fastest tuning for the current state (pbf_autotune)."""

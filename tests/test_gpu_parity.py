@@ -267,6 +267,51 @@ def test_tuning_never_changes_results(gpu, oracle_mod, tuning):
     assert_bits(v, ov, f"velocities with {tuning}")
 
 
+@pytest.mark.parametrize("extra", [dict(), dict(pair_list_capacity=0),
+                                   dict(coop_candidates=100), dict(pair_list_capacity=20)])
+def test_auto_sweeps_never_change_results(gpu, oracle_mod, extra):
+    """PBF_SWEEP_AUTO with a trial every few substeps: each trial steps one
+    real substep under each candidate configuration of the solver and
+    vorticity passes (masked, direct, cooperative, direct + cooperative), so
+    every configuration and every switch between them runs inside these 30
+    substeps, and the result is the oracle's bits."""
+    sc = scenes.plain_16k()
+    g = pg.SPH(sc.n, tuple(sc.params.grid), sc.params)
+    g.set_tuning(sweep_mode="auto", auto_period=2, **extra)
+    g.set_state(sc.x4, sc.v4)
+    assert g.sweep_choice() == {"solver": "coop", "vorticity": "coop", "trials": 0}
+    for _ in range(6):
+        g.step(5)
+    assert g.sweep_choice()["trials"] >= 3
+    o = run_oracle(oracle_mod, sc.params, sc.x4, sc.v4, 30)
+    x, v = g.get_state()
+    ox, ov = o.get_state()
+    assert_bits(x, ox, f"positions under automatic sweeps {extra}")
+    assert_bits(v, ov, f"velocities under automatic sweeps {extra}")
+
+
+def test_auto_is_the_default_and_resets(gpu):
+    """Handles default to PBF_SWEEP_AUTO, starting with the cooperative
+    sweeps below 32,768 particles and the masked sweeps from there; a state
+    upload restarts the trial schedule (the first trial after auto_period
+    substeps)."""
+    sc = scenes.plain_16k()
+    g = pg.SPH(sc.n, tuple(sc.params.grid), sc.params)
+    assert g.get_tuning().sweep_mode == 3
+    assert g.sweep_choice()["solver"] == "coop"
+    g.set_tuning(auto_period=8)
+    g.set_state(sc.x4, sc.v4)
+    g.step(8)
+    assert g.sweep_choice()["trials"] == 0
+    g.step(4)  # the trial's substeps: one per candidate
+    assert g.sweep_choice()["trials"] == 1
+    g.set_state(sc.x4, sc.v4)
+    assert g.sweep_choice() == {"solver": "coop", "vorticity": "coop", "trials": 0}
+    big = scenes.dam_break((40, 40, 40), (80, 80, 80), 4, 100, 0, "auto")
+    h = pg.SPH(big.n, tuple(big.params.grid), big.params)
+    assert h.sweep_choice()["solver"] == "masked"
+
+
 def test_lists_exact_in_a_calm_scene(gpu, oracle_mod):
     """A stable scene (reference default epsilon = 5) where the lists are in use on
     most sweeps, over many substeps."""
@@ -307,7 +352,7 @@ def test_block_size_and_autotune_never_change_results(gpu, oracle_mod):
     with pytest.raises(pg.PbfError):
         g.set_tuning(block_size=48)
     with pytest.raises(pg.PbfError):
-        g.set_tuning(sweep_mode=3)
+        g.set_tuning(sweep_mode=4)
 
 
 @pytest.mark.parametrize("after", [0, 1, 5, 12, 16])
