@@ -66,7 +66,11 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the backward/forward ratio")
     ap.add_argument("--no-splat", action="store_true", help="skip the depth/thickness splatting leg")
     ap.add_argument("--no-small", action="store_true", help="skip the 16,384-particle configuration")
-    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--autotune", action="store_true",
+                    help="fix the tuning pbf_autotune picks instead of the automatic sweep "
+                         "configuration")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="the default (kept for older command lines)")
     ap.add_argument("--recovery", action="store_true",
                     help="also run the 64-scene parameter recovery (about a minute)")
     return ap.parse_args()
@@ -416,7 +420,8 @@ def small_config(stream, with_cpu: bool):
     res = {"workload": sc.name, "particles": sc.n, "solver_iterations": it,
            "substeps": sc.substeps, "ms_per_step": ms / sc.substeps,
            "value": sc.n * it * sc.substeps / (ms * 1e-3), "unit": UNIT,
-           "ms_per_step_by_50": [ev[k].elapsed_time(ev[k + 1]) / seg for k in range(len(ev) - 1)]}
+           "ms_per_step_by_50": [ev[k].elapsed_time(ev[k + 1]) / seg for k in range(len(ev) - 1)],
+           "sweep_choice_after": sim.sweep_choice()}
     sim.close()
     if with_cpu:
         import oracle
@@ -515,11 +520,12 @@ def main():
     sim = pg.SPH(scene.n, tuple(scene.params.grid), scene.params)
     sim.set_stream(stream.cuda_stream)
 
-    # warm-up: the autotuner picks block size and neighbour-list settings on
-    # the first substeps of this scene (no setting changes any result), then
-    # W substeps under the chosen tuning capture the graph; reset after
+    # warm-up: with --autotune, the autotuner fixes block size, sweep mode and
+    # list settings on the first substeps of this scene (no setting changes
+    # any result); by default the handle's automatic sweep configuration runs.
+    # W substeps capture the graph; reset after
     sim.set_state(scene.x4, scene.v4)
-    tuning = sim.autotune(10) if not args.no_autotune else None
+    tuning = sim.autotune(10) if args.autotune else None
     sim.set_state(scene.x4, scene.v4)
     sim.step(W)
     sim.synchronize()
@@ -538,6 +544,8 @@ def main():
     sim.synchronize()  # surfaces any device status error
     ms = e0.elapsed_time(e1)
     clk = clocks.stop() if clocks else None
+    if tuning is None:
+        tuning = {"sweep_mode": "auto", "after_window": sim.sweep_choice()}
     t = torch.tensor([ms], device="cuda")
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -603,7 +611,7 @@ def main():
         ps.epsilon = 5.0
         sim.set_params(ps)
         sim.set_state(scene.x4, scene.v4)
-        stable_tuning = sim.autotune(10) if not args.no_autotune else None
+        stable_tuning = sim.autotune(10) if args.autotune else None
         sim.set_state(scene.x4, scene.v4)
         sim.step(3)
         sim.set_state(scene.x4, scene.v4)
@@ -616,6 +624,8 @@ def main():
         torch.cuda.synchronize()
         sim.synchronize()
         sms = g0.elapsed_time(g1)
+        if stable_tuning is None:
+            stable_tuning = {"sweep_mode": "auto", "after_run": sim.sweep_choice()}
         stable = {"value": scene.n * it * scene.substeps / (sms * 1e-3), "unit": UNIT,
                   "substeps": scene.substeps, "ms_per_step": sms / scene.substeps,
                   "epsilon": 5.0, "tuning": stable_tuning,

@@ -192,8 +192,16 @@ void reset_sweep_choice(pbf_sim* s) {
     s->auto_next = s->auto_period;
     s->auto_trial = -1;
     s->auto_trials = 0;
-    s->auto_cands = {PBF_PASS_MASKED, PBF_PASS_DIRECT, PBF_PASS_DIRECT_COOP};
+}
+
+// A trial's candidates: masked and direct always, the cooperative sweeps on
+// scenes small enough, and direct + cooperative once a pass has left the
+// masked configuration (in a calm state it costs ~2 substeps per trial).
+void pick_trial_candidates(pbf_sim* s) {
+    s->auto_cands = {PBF_PASS_MASKED, PBF_PASS_DIRECT};
     if (s->n < kCoopTrialBelow) s->auto_cands.push_back(PBF_PASS_COOP);
+    if (s->pass_solver != PBF_PASS_MASKED || s->pass_vort != PBF_PASS_MASKED)
+        s->auto_cands.push_back(PBF_PASS_DIRECT_COOP);
 }
 
 // SweepCfg modes (0 direct, 1 masked, 2 masked + pair lists, 3 cooperative)
@@ -950,7 +958,10 @@ pbf_status pbf_step(pbf_sim* s, uint32_t substeps) {
     const bool autom = s->tuning.sweep_mode == PBF_SWEEP_AUTO;
     uint32_t left = substeps;
     while (left > 0) {
-        if (autom && s->auto_trial < 0 && s->auto_count >= s->auto_next) s->auto_trial = 0;
+        if (autom && s->auto_trial < 0 && s->auto_count >= s->auto_next) {
+            pick_trial_candidates(s);
+            s->auto_trial = 0;
+        }
         if (autom && s->auto_trial >= 0) {
             pbf_status r = trial_substep(s);
             if (r != PBF_OK) return r;
