@@ -309,7 +309,8 @@ void free_sim(pbf_sim* s) {
                     s->VS, s->VX, s->OM,    s->Q,    s->keys,   s->skeys, s->perm,
                     s->cstart, s->cend, s->status, s->sort_mem, s->nbr_idx, s->nbr_cnt,
                     s->guard, s->d_consts, s->sid, s->sid_sorted, s->pair_idx, s->pair_cnt,
-                    s->scan_xy, s->scan_z, s->heavy, s->heavy_list, s->heavy_count};
+                    s->scan_xy, s->scan_z, s->heavy, s->heavy_list, s->heavy_count,
+                    s->runs};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (s->h_status) cudaFreeHost(s->h_status);
@@ -329,6 +330,13 @@ uint32_t kernels_per_substep(const pbf_sim* s) {
     const bool vort = s->params.vorticity_confinement != 0;
     uint32_t k = 1u /*predict*/ + 1u /*unmark*/ + 2u + passes /*sort*/ + 1u /*cells*/ +
                  2u * iters + 1u /*commit*/ + (vort ? 2u : 0u);
+    {  // run-start bits after each delta-p whose positions a direct sweep reads next
+        const PassModes a = modes_of(s, s->pass_solver), b = modes_of(s, s->pass_vort);
+        const bool lists = skin_lists_on(s);
+        const bool rs = !lists && (a.first == 0 || a.second == 0);
+        const bool rv = !lists && vort && (b.first == 0 || b.second == 0);
+        if (iters > 0) k += (iters - 1) * (rs ? 1u : 0u) + (rv ? 1u : 0u);
+    }
     if (mixed_on(s)) {  // the flag pass and a cooperative launch after each one-thread sweep
         const PassModes a = modes_of(s, s->pass_solver), b = modes_of(s, s->pass_vort);
         k += 1u + iters * ((a.first != 3) + (a.second != 3)) +
@@ -494,8 +502,10 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
     // 3 cell ranges (NeighbourCellFinder::FindNeighbourCells)
     const size_t half = ((size_t)n + 1) / 2;
     auto scan_set = [&](int k) { return ScanPos{s->scan_xy + k * half, s->scan_z + k * half}; };
-    k_find_cells<<<g, kBlock, 0, st>>>(s->skeys, s->perm, s->xstar, s->XP, n, s->ncells, s->cstart,
-                                       s->cend, s->status + 1, s->sid, s->sid_sorted, scan_set(0));
+    // (over n + 1 threads: the run-start bits end with a terminator at n)
+    k_find_cells<<<grid_for(n + 1), kBlock, 0, st>>>(s->skeys, s->perm, s->xstar, s->XP, n,
+                                                     s->ncells, s->cstart, s->cend, s->status + 1,
+                                                     s->sid, s->sid_sorted, scan_set(0), s->runs);
     // mixed sweeps: flag the particles with more than coop_candidates stencil
     // candidates; the cooperative kernels sweep those, the others skip them
     const bool mixed = mixed_on(s);
@@ -509,8 +519,13 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
     // 4 solver iterations (calclambda / updatepos).  The first lambda sweep
     // also records the neighbour lists the later sweeps replay.
     const NbrLists nl{s->nbr_idx, s->nbr_cnt, s->guard, s->nbr_cap, n};
+    // the direct sweeps skip runs of coincident candidates (neighbours.cuh:
+    // visit_direct_piles); run-start bits of each position set they read
+    const bool runs_solver = !lists && (ms.first == 0 || ms.second == 0);
+    const bool runs_vort = !lists && vort && (mv.first == 0 || mv.second == 0);
     const PairLists pl{s->pair_idx, s->pair_cnt, s->pair_cap, n, mixed ? s->heavy : nullptr,
-                       s->heavy_list, s->heavy_count};
+                       s->heavy_list, s->heavy_count,
+                       runs_solver || runs_vort ? s->runs : nullptr};
     cudaError_t ge = cudaMemsetAsync(s->guard, 0, sizeof(uint32_t) * (2 + iters), st);
     if (ge != cudaSuccess) return ge;
     const float4* cur = s->XP;
@@ -534,6 +549,8 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
         launch_delta_p(s_dp, st, Lk, s->XP, s->skeys, s->cstart, s->cend, nxt, nl, pl,
                        scan_set(cur_set), write_scan ? scan_set(nxt_set) : ScanPos{nullptr, nullptr},
                        in_slot, (int)it + 1, n, cps, s->status);
+        if (it + 1 < iters ? runs_solver : runs_vort)
+            k_run_flags<<<grid_for(n + 1), kBlock, 0, st>>>(nxt, n, s->runs);
         mark(5 + 2 * it);
         cur = nxt;
         cur_set = nxt_set;
@@ -658,7 +675,7 @@ pbf_status pbf_create_batch(const pbf_params* scene_params, const uint32_t* scen
     ALLOC(VS, n) ALLOC(VX, n) ALLOC(OM, n) ALLOC(Q, n) ALLOC(keys, n) ALLOC(skeys, n)
     ALLOC(perm, n) ALLOC(cstart, s->ncells) ALLOC(cend, s->ncells) ALLOC(status, 2)
     ALLOC(scan_xy, 3 * (((size_t)n + 1) / 2)) ALLOC(scan_z, 3 * (((size_t)n + 1) / 2))
-    ALLOC(heavy, n) ALLOC(heavy_list, n) ALLOC(heavy_count, 1)
+    ALLOC(heavy, n) ALLOC(heavy_list, n) ALLOC(heavy_count, 1) ALLOC(runs, (size_t)n / 32 + 2)
     if (num_scenes > 1) {
         ALLOC(d_consts, num_scenes) ALLOC(sid, n) ALLOC(sid_sorted, n)
     }
@@ -1088,7 +1105,7 @@ pbf_status pbf_compute_diagnostics(pbf_sim* s, pbf_diagnostics* out) {
     if (e != cudaSuccess) return cuda_fail(s, e, "diagnostics sort");
     k_find_cells<<<g, kBlock, 0, st>>>(s->skeys, s->perm, s->xstar, s->XP, n, s->ncells, s->cstart,
                                        s->cend, s->status + 1, s->sid, s->sid_sorted,
-                                       ScanPos{nullptr, nullptr});
+                                       ScanPos{nullptr, nullptr}, nullptr);
     if (s->nscenes == 1)
         launch_diagnostics(g, st, s->XP, s->v, s->skeys, s->perm, s->cstart, s->cend,
                                             s->VX, n, OneScene{s->dc});
@@ -1185,7 +1202,7 @@ pbf_status pbf_find_cells(const uint32_t* sorted_keys, uint32_t n, uint32_t num_
     if (e == cudaSuccess && n > 0) {
         k_find_cells<<<grid_for(n), kBlock, 0, st>>>(sorted_keys, nullptr, nullptr, nullptr, n,
                                                      num_cells, start, end, bad, nullptr, nullptr,
-                                                     ScanPos{nullptr, nullptr});
+                                                     ScanPos{nullptr, nullptr}, nullptr);
         e = cudaGetLastError();
     }
     uint32_t hbad = 0;

@@ -72,6 +72,9 @@ struct PairLists {
     const uint8_t* heavy = nullptr;  // mixed sweeps: particles the cooperative kernels take
     const uint32_t* heavy_list = nullptr;   // their sorted indices
     const uint32_t* heavy_count = nullptr;  // and how many there are
+    // run-start bits of the sweep's position set (neighbours.cuh: runs), read
+    // by the direct sweeps' coincident runs; NULL: no run path
+    const uint32_t* runs = nullptr;
 };
 
 // Scan copy of a sorted position array, read by the masked stencil scans two

@@ -56,6 +56,107 @@ __device__ __forceinline__ void visit_full(uint32_t i, uint32_t key, const DevCo
             if ((uint32_t)j != i) f((uint32_t)j);
 }
 
+// Runs of equal positions in sorted order.  Bit j of `runs` (32 per word) is
+// set when sorted particle j starts a run: j == 0, its position differs
+// (bitwise x, y, z) from particle j - 1's in the sweep's position set, j is a
+// multiple of kRunStride (so a search for the next start reads at most
+// kRunStride / 32 words) or j >= n (the terminator).  Built once per position
+// set by k_run_flags / k_find_cells.
+constexpr uint32_t kRunStride = 1024;
+
+// First run start after j (a set bit > j exists: the terminator at n).
+__device__ __forceinline__ uint32_t run_end(const uint32_t* __restrict__ runs, uint32_t j) {
+    const uint32_t k = j + 1u;
+    uint32_t w = k >> 5;
+    uint32_t word = __ldg(runs + w) & (0xFFFFFFFFu << (k & 31u));
+    while (word == 0u) word = __ldg(runs + ++w);
+    return (w << 5) + (uint32_t)(__ffs((int)word) - 1);
+}
+
+// Cells of at least this many particles take the run path; runs of at least
+// kRunMin candidates go to `uniform` as a whole.
+constexpr int32_t kPileMin = 32;
+constexpr uint32_t kRunMin = 4;
+
+// visit_full's order, cell by cell, with runs of equal positions.  The box
+// clamp stacks particles on single points (the box corners: by substep 300
+// of the 2M dam break one corner cell holds 130,498 particles at one
+// position).  In a cell of at least kPileMin particles, a candidate j that
+// starts or continues a run of equal positions is tested first; the run
+// [j, r) ends at the next run start or the cell's end, and every candidate in
+// it is at the same offset d (r2) from particle i:
+//  - r2 == 0: each candidate other than i gives the coincident term (len 0):
+//    `coincident(j, r, m)` receives the run and the count of those;
+//  - otherwise (i is not in the run), if it holds at least kRunMin
+//    candidates and r2 is not NaN: `uniform(j, r, d, r2)` accumulates their
+//    terms in order;
+//  - otherwise f runs on each.
+// The visit then resumes at r.  Every other candidate goes to f.  pos(j) is
+// the position the sweep tests at (the set `runs` was built from).
+template <class Pos, class F, class G, class U>
+__device__ __forceinline__ void visit_direct_piles(uint32_t i, uint32_t key, const DevConsts& c,
+                                                   const int32_t* __restrict__ cstart,
+                                                   const int32_t* __restrict__ cend,
+                                                   const uint32_t* __restrict__ runs, Pos&& pos,
+                                                   float3 pi, F&& f, G&& coincident,
+                                                   U&& uniform) {
+    const uint32_t Gx = c.Gi[0], Gy = c.Gi[1], Gz = c.Gi[2];
+    const uint32_t local = key - c.cell_base;
+    const int cx = (int)(local % Gx);
+    const uint32_t rem = local / Gx;
+    const int cz = (int)(rem % Gz);
+    const int cy = (int)(rem / Gz);
+    const int xlo = cx > 0 ? cx - 1 : 0;
+    const int xhi = cx + 1 < (int)Gx ? cx + 1 : (int)Gx - 1;
+#pragma unroll 1
+    for (int o = 0; o < 9; ++o) {
+        const int ny = cy + (o / 3) - 1, nz = cz + (o % 3) - 1;
+        if (ny < 0 || ny >= (int)Gy || nz < 0 || nz >= (int)Gz) continue;
+        const uint32_t base = c.cell_base + (uint32_t)ny * c.GxGz + (uint32_t)nz * Gx;
+        int32_t b = -1, e = -1;  // the row's run, as visit_full merges it
+#pragma unroll 1
+        for (int xx = xlo; xx <= xhi; ++xx) {
+            const uint32_t cell = base + (uint32_t)xx;
+            const int32_t s = __ldg(cstart + cell);
+            if (s == -1) continue;
+            const int32_t t = __ldg(cend + cell);
+            if (t - s < kPileMin) {
+                if (b == -1) b = s;
+                e = t;
+                continue;
+            }
+            // a large cell: first the small cells before it, then its runs
+            for (int32_t j = b; j < e; ++j)
+                if ((uint32_t)j != i) f((uint32_t)j);
+            b = e = -1;
+            for (uint32_t j = (uint32_t)s; j < (uint32_t)t;) {
+                const uint32_t k = j + 1u;
+                const bool in_run = k < (uint32_t)t && !((__ldg(runs + (k >> 5)) >> (k & 31u)) & 1u);
+                if (in_run) {
+                    const float3 d = sub3(pi, pos(j));
+                    const float r2 = dot3(d, d);
+                    uint32_t r = run_end(runs, j);
+                    if (r > (uint32_t)t) r = (uint32_t)t;
+                    if (r2 == 0.0f) {
+                        coincident(j, r, (r - j) - ((j <= i && i < r) ? 1u : 0u));
+                        j = r;
+                        continue;
+                    }
+                    if (r - j >= kRunMin && r2 == r2) {
+                        uniform(j, r, d, r2);
+                        j = r;
+                        continue;
+                    }
+                }
+                if (j != i) f(j);
+                ++j;
+            }
+        }
+        for (int32_t j = b; j < e; ++j)
+            if ((uint32_t)j != i) f((uint32_t)j);
+    }
+}
+
 // Spreads the low 16 bits of x to the even bit positions.
 __device__ __forceinline__ uint32_t spread_even(uint32_t x) {
     x = (x | (x << 8)) & 0x00FF00FFu;

@@ -60,6 +60,9 @@ struct pbf_sim {
     uint8_t* heavy = nullptr;
     uint32_t* heavy_list = nullptr;
     uint32_t* heavy_count = nullptr;
+    // run-start bits of the position set the direct sweeps read (k_find_cells,
+    // k_run_flags), n / 32 + 2 words
+    uint32_t* runs = nullptr;
     // scan copies (ScanPos) of the predicted positions (set 0) and of the
     // solver iterates (sets 1 and 2, alternating), (n + 1) / 2 pairs per set
     float4* scan_xy = nullptr;

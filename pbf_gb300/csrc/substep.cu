@@ -21,6 +21,7 @@
 #include <type_traits>
 
 #include "substep.cuh"
+#include "repeat_add.h"
 #include "neighbours.cuh"
 
 namespace pbf {
@@ -69,6 +70,33 @@ k_unmark_cells(const uint32_t* __restrict__ prev_sorted, uint32_t n, uint32_t nc
     if (k < ncells && (i == 0 || prev_sorted[i - 1] != k)) cstart[k] = -1;
 }
 
+// The run-start bit of sorted particle j (neighbours.cuh: runs) from its
+// position p and the previous particle's q, with the warp's 32 bits stored
+// by its first lane.  Call with every lane of the warp.
+__device__ __forceinline__ void store_run_bits(uint32_t j, uint32_t n, float3 p, float3 q,
+                                               uint32_t* __restrict__ runs) {
+    const bool start = j == 0u || j >= n || j % kRunStride == 0u ||
+                       __float_as_uint(p.x) != __float_as_uint(q.x) ||
+                       __float_as_uint(p.y) != __float_as_uint(q.y) ||
+                       __float_as_uint(p.z) != __float_as_uint(q.z);
+    const uint32_t word = __ballot_sync(0xFFFFFFFFu, start);
+    // words 0 .. n / 32 exist (n / 32 + 2 are allocated); later warps write none
+    if ((threadIdx.x & 31u) == 0u && (j >> 5) <= (n >> 5)) runs[j >> 5] = word;
+}
+
+// Run-start bits of a position set, indices 0..n (launch over n + 1 threads
+// in whole warps).
+__global__ void __launch_bounds__(kBlock)
+k_run_flags(const float4* __restrict__ P, uint32_t n, uint32_t* __restrict__ runs) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    float3 p = make_float3(0.0f, 0.0f, 0.0f), q = p;
+    if (j < n) {
+        p = xyz(__ldg(P + j));
+        if (j > 0) q = xyz(__ldg(P + j - 1));
+    }
+    store_run_bits(j, n, p, q, runs);
+}
+
 // findcells.glsl:34-53 (start of cell(x_0) = 0 and end of cell(x_{n-1}) = n)
 // fused with the gather of the predicted positions into sorted order.
 // Keys >= ncells are skipped and reported through `status` (bad input only).
@@ -76,15 +104,28 @@ __global__ void __launch_bounds__(kBlock)
 k_find_cells(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
              const float4* __restrict__ xstar, float4* __restrict__ P0, uint32_t n, uint32_t ncells,
              int32_t* __restrict__ cstart, int32_t* __restrict__ cend, uint32_t* bad,
-             const uint32_t* __restrict__ sid, uint32_t* __restrict__ sid_sorted, ScanPos sx) {
+             const uint32_t* __restrict__ sid, uint32_t* __restrict__ sid_sorted, ScanPos sx,
+             uint32_t* __restrict__ runs) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t k = skeys[i];
-    if (P0) {
-        const float4 p = __ldg(xstar + perm[i]);
+    const bool valid = i < n;
+    float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (valid && P0) {
+        p = __ldg(xstar + perm[i]);
         P0[i] = p;
         if (sx.xy) scanpos_store(sx, i, p.x, p.y, p.z);
     }
+    if (runs && P0) {
+        // run-start bits of the predicted positions (launched over n + 1
+        // threads); the previous particle's position is the previous lane's,
+        // or a load on a warp's first lane
+        float3 q = make_float3(__shfl_up_sync(0xFFFFFFFFu, p.x, 1),
+                               __shfl_up_sync(0xFFFFFFFFu, p.y, 1),
+                               __shfl_up_sync(0xFFFFFFFFu, p.z, 1));
+        if ((threadIdx.x & 31u) == 0u && valid && i > 0) q = xyz(__ldg(xstar + perm[i - 1]));
+        store_run_bits(i, n, xyz(p), q, runs);
+    }
+    if (!valid) return;
+    const uint32_t k = skeys[i];
     if (sid_sorted) sid_sorted[i] = __ldg(sid + perm[i]);
     if (k >= ncells) {
         atomicOr(bad, 1u);
@@ -239,6 +280,21 @@ __device__ __forceinline__ void lambda_pair(const DevConsts& c, float3 d, float 
     a.gi = add3(a.gi, g);                  // :93
 }
 
+// lambda_pair for m neighbours at the same offset d (a run of equal
+// positions): each of the four sums receives its term m times, as m calls
+// would add it (repeat_add: the same bits).
+__device__ __forceinline__ void lambda_pair_run(const DevConsts& c, float3 d, float r2,
+                                                uint32_t m, LambdaAcc& a) {
+    if (r2 > c.r2cut) return;
+    const float len = fsqrt(r2);
+    a.rho = repeat_add(a.rho, w_poly6(c, len), m);  // :80-82
+    if (len == 0.0f) return;
+    const float3 g = scale3(d, grad_scale(c.kg_lambda, c.h, len));  // :86-87
+    a.sumk = repeat_add(a.sumk, dot3(g, g), m);                      // :89
+    a.gi = make_float3(repeat_add(a.gi.x, g.x, m), repeat_add(a.gi.y, g.y, m),
+                       repeat_add(a.gi.z, g.z, m));  // :93
+}
+
 // What the adjoint needs of a lambda evaluation: sum_j grad_pj C_i (the
 // gradient w.r.t. p_i, calclambda.glsl:93) and the full denominator sum
 // before epsilon (:89,97).
@@ -260,6 +316,10 @@ __device__ __forceinline__ float lambda_finish(const DevConsts& c, const LambdaA
 // 6 or 4 blocks with more registers measured slower).  One thread per sorted
 // particle.
 constexpr int kSweepBlocksPerSM = 8;
+// The direct first vorticity pass carries the run path's extra state (its
+// velocity loops over coincident and equal-offset runs): 6 blocks per SM
+// (40 registers) keep it from spilling in those loops.
+constexpr int kDirectVortBlocksPerSM = 6;
 
 // Instantiations of the sweep kernels (pbf_tuning): MODE is the stencil scan
 // (kDirect: the reference's loop shape; kMasked: masked scans; kPairs: masked
@@ -312,16 +372,37 @@ k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys
                 visit_masked<false>(i, skeys[i], c, cstart, cend, sx, pi,
                                     [](int32_t, uint32_t) {}, eval);
         } else {
-            visit_full(i, skeys[i], c, cstart, cend, [&](uint32_t j) {
-                const float3 d = sub3(pi, xyz(__ldg(XP + j)));
-                const float r2 = dot3(d, d);
-                if (LISTS && r2 <= c.r2list) {
-                    if ((uint32_t)cnt < cap) nl.idx[(size_t)cnt * n + i] = j;
-                    ++cnt;
+            bool piles = false;
+            if constexpr (!LISTS) {
+                if (pw.runs) {
+                    // a coincident neighbour adds W(0) to the density (:80-82)
+                    visit_direct_piles(
+                        i, skeys[i], c, cstart, cend, pw.runs,
+                        [&](uint32_t j) { return xyz(__ldg(XP + j)); }, pi,
+                        [&](uint32_t j) {
+                            const float3 d = sub3(pi, xyz(__ldg(XP + j)));
+                            const float r2 = dot3(d, d);
+                            if (r2 > c.r2cut) return;
+                            lambda_pair(c, d, r2, a);
+                        },
+                        [&](uint32_t, uint32_t, uint32_t m) { a.rho = repeat_add(a.rho, w_poly6(c, 0.0f), m); },
+                        [&](uint32_t j0, uint32_t r, float3 d, float r2) {
+                            lambda_pair_run(c, d, r2, r - j0, a);
+                        });
+                    piles = true;
                 }
-                if (r2 > c.r2cut) return;
-                lambda_pair(c, d, r2, a);
-            });
+            }
+            if (!piles)
+                visit_full(i, skeys[i], c, cstart, cend, [&](uint32_t j) {
+                    const float3 d = sub3(pi, xyz(__ldg(XP + j)));
+                    const float r2 = dot3(d, d);
+                    if (LISTS && r2 <= c.r2list) {
+                        if ((uint32_t)cnt < cap) nl.idx[(size_t)cnt * n + i] = j;
+                        ++cnt;
+                    }
+                    if (r2 > c.r2cut) return;
+                    lambda_pair(c, d, r2, a);
+                });
         }
         if (LISTS) nl.cnt[i] = (uint32_t)cnt <= cap ? cnt : -1;
         L[i] = make_float4(pi.x, pi.y, pi.z, lambda_finish(c, a));
@@ -374,6 +455,14 @@ k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
         if constexpr (MODE == kPairs)
             scan_then_eval<false>(i, skeys[i], c, cstart, cend, sx, pi, pw, [](int32_t, uint32_t) {},
                                   eval);
+        else if (MODE == kDirect && !LISTS && pw.runs)
+            visit_direct_piles(
+                i, skeys[i], c, cstart, cend, pw.runs,
+                [&](uint32_t j) { return xyz(__ldg(P + j)); }, pi, eval,
+                [&](uint32_t, uint32_t, uint32_t m) { a.rho = repeat_add(a.rho, w_poly6(c, 0.0f), m); },
+                [&](uint32_t j0, uint32_t r, float3 d, float r2) {
+                    lambda_pair_run(c, d, r2, r - j0, a);
+                });
         else
             sweep_visit<MODE == kMasked>(i, skeys[i], c, cstart, cend, sx, pi, eval);
     }
@@ -426,7 +515,26 @@ k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
                     listed = true;
                 }
             }
-            if (!listed) sweep_visit<MODE != kDirect>(i, skeys[i], c, cstart, cend, sx, pi, body);
+            if (!listed) {
+                if (MODE == kDirect && !LISTS && pr.runs)  // coincident: no term (:56)
+                    visit_direct_piles(
+                        i, skeys[i], c, cstart, cend, pr.runs,
+                        [&](uint32_t j) { return xyz(__ldg(L + j)); }, pi, body, [](uint32_t, uint32_t, uint32_t) {},
+                        [&](uint32_t j0, uint32_t r, float3 d, float r2) {
+                            // the same offset for the run: only lambda_j differs
+                            if (r2 > c.r2cut) return;
+                            const float len = fsqrt(r2);
+                            float sc = fmul(c.scale, w_poly6(c, len));  // :57
+                            sc = fmul(sc, sc);                           // :58
+                            sc = fmul(sc, sc);                           // :59
+                            sc = fmul(c.negk, sc);                       // :60
+                            const float3 g = scale3(d, grad_scale(c.kg, c.h, len));
+                            for (uint32_t j = j0; j < r; ++j)
+                                dp = fma3(fadd(fadd(li, __ldg(&L[j].w)), sc), g, dp);  // :65
+                        });
+                else
+                    sweep_visit<MODE != kDirect>(i, skeys[i], c, cstart, cend, sx, pi, body);
+            }
         }
         float3 q = fma3(c.oorho, dp, pi);  // :85
         // clamp (:100) as min(max(q, lo), hi) with explicit selects, so signed
@@ -739,7 +847,7 @@ k_commit(const float4* __restrict__ P, const uint32_t* __restrict__ perm, float4
 // vorticity.glsl:34-60: XSPH velocity and the vorticity vector, Jacobi
 // (every read sees the committed velocities).
 template <class CP, int MODE, bool LISTS>
-__global__ void __launch_bounds__(kBlock, kSweepBlocksPerSM)
+__global__ void __launch_bounds__(kBlock, MODE == kDirect ? kDirectVortBlocksPerSM : kSweepBlocksPerSM)
 k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
               const float4* __restrict__ VS, const uint32_t* __restrict__ skeys,
               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
@@ -784,6 +892,26 @@ k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
         if constexpr (MODE == kPairs)
             scan_then_eval<false>(i, skeys[i], c, cstart, cend, sx, pi, pw, [](int32_t, uint32_t) {},
                                   eval);
+        else if (MODE == kDirect && !LISTS && pw.runs)
+            visit_direct_piles(
+                i, skeys[i], c, cstart, cend, pw.runs,
+                [&](uint32_t j) { return xyz(__ldg(P + j)); }, pi, eval,
+                [&](uint32_t j0, uint32_t r, uint32_t) {  // len 0: W(0) (v_j - v_i), no curl
+                    const float w0 = w_poly6(c, 0.0f);
+                    for (uint32_t j = j0; j < r; ++j)
+                        if (j != i) acc = fma3(w0, sub3(xyz(__ldg(VS + j)), vi), acc);
+                },
+                [&](uint32_t j0, uint32_t r, float3 d, float r2) {  // one offset: v_j differs
+                    if (r2 > c.r2cut) return;
+                    const float len = fsqrt(r2);
+                    const float wl = w_poly6(c, len);
+                    const float3 g = scale3(d, grad_scale(c.kg, c.h, len));
+                    for (uint32_t j = j0; j < r; ++j) {
+                        const float3 vij = sub3(xyz(__ldg(VS + j)), vi);  // :50
+                        acc = fma3(wl, vij, acc);                         // :52-54
+                        w = add3(w, cross3(vij, g));                      // :55
+                    }
+                });
         else
             sweep_visit<MODE == kMasked>(i, skeys[i], c, cstart, cend, sx, pi, eval);
     }
@@ -828,7 +956,21 @@ k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ XP,
                 listed = true;
             }
         }
-        if (!listed) sweep_visit<MODE != kDirect>(i, skeys[i], c, cstart, cend, sx, pi, body);
+        if (!listed) {
+            if (MODE == kDirect && !LISTS && pr.runs)  // coincident: no term (:71)
+                visit_direct_piles(
+                    i, skeys[i], c, cstart, cend, pr.runs,
+                    [&](uint32_t j) { return xyz(__ldg(Q + j)); }, pi, body, [](uint32_t, uint32_t, uint32_t) {},
+                    [&](uint32_t j0, uint32_t r, float3 d, float r2) {
+                        // the same offset for the run: only |omega_j| differs
+                        if (r2 > c.r2cut) return;
+                        const float3 g = scale3(d, grad_scale(c.kg, c.h, fsqrt(r2)));
+                        for (uint32_t j = j0; j < r; ++j)
+                            eta = fma3(__ldg(&Q[j].w), g, eta);  // :72
+                    });
+            else
+                sweep_visit<MODE != kDirect>(i, skeys[i], c, cstart, cend, sx, pi, body);
+        }
     }
     if (eta_out) eta_out[i] = make_float4(eta.x, eta.y, eta.z, 0.0f);
     const float l = fsqrt(dot3(eta, eta));  // :76

@@ -8,12 +8,13 @@ namespace pbf {
 
 __global__ void k_unmark_cells(const uint32_t* __restrict__ prev_sorted, uint32_t n,
                                uint32_t ncells, int32_t* __restrict__ cstart);
+__global__ void k_run_flags(const float4* __restrict__ P, uint32_t n, uint32_t* __restrict__ runs);
 __global__ void k_find_cells(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
                              const float4* __restrict__ xstar, float4* __restrict__ P0, uint32_t n,
                              uint32_t ncells, int32_t* __restrict__ cstart,
                              int32_t* __restrict__ cend, uint32_t* bad,
                              const uint32_t* __restrict__ sid, uint32_t* __restrict__ sid_sorted,
-                             ScanPos sx);
+                             ScanPos sx, uint32_t* __restrict__ runs);
 
 // Host launchers of the templated stage kernels (explicitly instantiated for
 // OneScene and ManyScenes in substep.cu).  The neighbour-sweep launchers take
