@@ -62,6 +62,8 @@ def parse():
                     help="full substeps of the CPU baseline sample")
     ap.add_argument("--e2e-steps", type=int, default=0, help="0: min(steps, 50)")
     ap.add_argument("--no-stable", action="store_true", help="skip the epsilon = 5 full run")
+    ap.add_argument("--no-full", action="store_true",
+                    help="skip the full 500-substep run of the workload itself")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-scene comparison")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the backward/forward ratio")
     ap.add_argument("--no-splat", action="store_true", help="skip the depth/thickness splatting leg")
@@ -254,18 +256,22 @@ def splat_leg(stream, reps: int = 20):
     return res
 
 
-def adjoint_ratio(stream, substeps: int = 64, every: int = 8):
+def adjoint_ratio(stream, substeps: int = 64, every: int = 8, epsilon=None):
     """Backward / forward time of the differentiable scene: 32,768 particles
     (32^3 lattice) in a 64^3 box, velocities N(0, 0.25^2) from seed A, 64
     substeps x 4 iterations; loss = mean squared distance of the final
     positions to those of a run from seed-B velocities.  Forward = the
     recorded run (checkpoint every 8 substeps); backward = recomputing each
-    8-substep segment with its tape plus the adjoint kernels."""
+    8-substep segment with its tape plus the adjoint kernels.  `epsilon`
+    replaces the CFM epsilon of both runs (None: the workload's 0.01)."""
     import torch
     import numpy as np
     import pbf_gb300 as pg
     from pbf_gb300 import scenes
     a, b = scenes.diff_32k()
+    if epsilon is not None:
+        a.params.epsilon = epsilon
+        b.params.epsilon = epsilon
     n = a.n
     tgt = pg.SPH(n, tuple(b.params.grid), b.params)
     tgt.set_state(b.x4, b.v4)
@@ -306,9 +312,12 @@ def adjoint_ratio(stream, substeps: int = 64, every: int = 8):
             "grad_norm_v0": float(np.linalg.norm(dv0[:, :3])),
             "grad_finite": bool(np.all(np.isfinite(dv0))),
             "grad_params": dict(zip(pg.SPH.PARAM_NAMES, [float(v) for v in g[0]])),
+            "epsilon": float(a.params.epsilon),
             "note": "wall-clock per call, host synchronised; backward includes the "
-                    "recomputation of every checkpoint segment; with epsilon = 0.01 the "
-                    "64-substep derivative overflows FP32 (the run blows up)"}
+                    "recomputation of every checkpoint segment" +
+                    ("" if epsilon is not None else
+                     "; with epsilon = 0.01 the 64-substep derivative overflows FP32 (the "
+                     "run blows up: see adjoint_32k_epsilon_5 for finite gradients)")}
 
 
 def recovery(stream, num_scenes: int = 64, substeps: int = 32, steps: int = 50, seed: int = 11,
@@ -633,9 +642,35 @@ def main():
                           "(src/SPH.cpp:138), full run"}
         sim.set_params(scene.params)
 
-    adjoint = None
+    # the workload's own full run (epsilon = 0.01, all substeps): the fluid
+    # collapses into dense clumps and corner piles after ~100 substeps, where
+    # the automatic sweep configuration moves to the direct sweeps
+    full = None
+    if not args.no_full:
+        sim.set_state(scene.x4, scene.v4)
+        torch.cuda.synchronize()
+        seg = 100
+        fev = [torch.cuda.Event(enable_timing=True) for _ in range(scene.substeps // seg + 1)]
+        fev[0].record(stream)
+        for k in range(scene.substeps // seg):
+            sim.step(seg)
+            fev[k + 1].record(stream)
+        torch.cuda.synchronize()
+        sim.synchronize()
+        fms = fev[0].elapsed_time(fev[-1])
+        full = {"value": scene.n * it * scene.substeps / (fms * 1e-3), "unit": UNIT,
+                "substeps": scene.substeps, "ms_per_step": fms / scene.substeps,
+                "ms_per_step_by_100": [fev[k].elapsed_time(fev[k + 1]) / seg
+                                       for k in range(len(fev) - 1)],
+                "sweep_choice_after": sim.sweep_choice(),
+                "state_after": sim.diagnostics(),
+                "note": "graph replay with the default automatic sweep configuration "
+                        "(its trials are real substeps of the run)"}
+
+    adjoint = adjoint5 = None
     if not args.no_adjoint:
         adjoint = adjoint_ratio(stream)
+        adjoint5 = adjoint_ratio(stream, epsilon=5.0)
     splats = None
     if not args.no_splat:
         splats = splat_leg(stream)
@@ -685,8 +720,10 @@ def main():
             "kernel_share": {k: v / total_stage for k, v in stages.items()},
             "gpu_launches": launches,
             "stable_500": stable,
+            "full_500": full,
             "batched_256": batched,
             "adjoint_32k": adjoint,
+            "adjoint_32k_epsilon_5": adjoint5,
             "splat_reference_scene": splats,
             "dam_break_16k_200": small,
             "state_after_window": state_after,
