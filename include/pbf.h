@@ -276,8 +276,14 @@ pbf_status pbf_get_timing(pbf_sim* sim, float ms[5]);
  * per-kernel split of the phases above. */
 pbf_status pbf_get_stage_times(pbf_sim* sim, double ms_sum[8], uint32_t* substeps);
 
-/* Number of kernels one substep launches (for launch accounting). */
+/* Number of kernels one substep launches under the current sweep
+ * configuration (for launch accounting). */
 uint32_t pbf_kernels_per_substep(const pbf_sim* sim);
+/* Kernels launched by all substeps of this handle so far (graph replays,
+ * automatic-mode trials and timed substeps, each counted under the
+ * configuration it ran); the difference around a window counts its
+ * launches.  No reference counterpart. */
+uint64_t pbf_kernels_launched(const pbf_sim* sim);
 
 /* ---- debug reads of the last substep's intermediates (synchronising) -------- */
 

@@ -127,6 +127,7 @@ SIGNATURES = {
     "pbf_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
     "pbf_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
     "pbf_get_sweep_choice": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
+    "pbf_kernels_launched": (C.c_uint64, [_P]),
     "pbf_autotune": (C.c_int, [_P, C.c_uint32, C.POINTER(Tuning)]),
     "pbf_device_status": (C.c_int, [_P, _U32P]),
     "pbf_enable_timing": (C.c_int, [_P, C.c_int]),

@@ -367,6 +367,7 @@ pbf_status launch_graph(pbf_sim* s, uint32_t count) {
         PBF_CUDA(s, cudaGraphInstantiate(&s->execs[key], g, 0));
     }
     for (uint32_t k = 0; k < count; ++k) PBF_CUDA(s, cudaGraphLaunch(s->execs[key], s->stream));
+    s->launched += (uint64_t)count * kernels_per_substep(s);
     return PBF_OK;
 }
 
@@ -389,6 +390,7 @@ pbf_status trial_substep(pbf_sim* s) {
     const int k = s->auto_trial;
     s->pass_solver = s->pass_vort = s->auto_cands[k];
     cudaError_t e = enqueue_substep(s, s->trial_ev.data() + per * k);
+    s->launched += kernels_per_substep(s);
     s->pass_solver = keep_s;
     s->pass_vort = keep_v;
     if (e != cudaSuccess) return cuda_fail(s, e, "trial substep launch");
@@ -433,6 +435,7 @@ pbf_status timed_substep(pbf_sim* s) {
     }
     cudaError_t e = enqueue_substep(s, s->ev.data());
     if (e != cudaSuccess) return cuda_fail(s, e, "substep launch");
+    s->launched += kernels_per_substep(s);
     PBF_CUDA(s, cudaEventSynchronize(s->ev[need - 1]));
     auto span = [&](size_t a, size_t b) {
         float m = 0.0f;
@@ -505,7 +508,8 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
     // (over n + 1 threads: the run-start bits end with a terminator at n)
     k_find_cells<<<grid_for(n + 1), kBlock, 0, st>>>(s->skeys, s->perm, s->xstar, s->XP, n,
                                                      s->ncells, s->cstart, s->cend, s->status + 1,
-                                                     s->sid, s->sid_sorted, scan_set(0), s->runs);
+                                                     s->sid, s->sid_sorted, scan_set(0), s->runs,
+                                                     s->status);
     // mixed sweeps: flag the particles with more than coop_candidates stencil
     // candidates; the cooperative kernels sweep those, the others skip them
     const bool mixed = mixed_on(s);
@@ -1037,6 +1041,8 @@ pbf_status pbf_get_stage_times(pbf_sim* s, double ms_sum[8], uint32_t* substeps)
 
 uint32_t pbf_kernels_per_substep(const pbf_sim* s) { return s ? kernels_per_substep(s) : 0; }
 
+uint64_t pbf_kernels_launched(const pbf_sim* s) { return s ? s->launched : 0; }
+
 pbf_status pbf_get_timing(pbf_sim* s, float ms[5]) {
     if (!s || !ms) return fail(s, PBF_ERR_INVALID_ARGUMENT, "NULL argument");
     for (int p = 0; p < 5; ++p) ms[p] = s->ms[p];
@@ -1105,7 +1111,7 @@ pbf_status pbf_compute_diagnostics(pbf_sim* s, pbf_diagnostics* out) {
     if (e != cudaSuccess) return cuda_fail(s, e, "diagnostics sort");
     k_find_cells<<<g, kBlock, 0, st>>>(s->skeys, s->perm, s->xstar, s->XP, n, s->ncells, s->cstart,
                                        s->cend, s->status + 1, s->sid, s->sid_sorted,
-                                       ScanPos{nullptr, nullptr}, nullptr);
+                                       ScanPos{nullptr, nullptr}, nullptr, nullptr);
     if (s->nscenes == 1)
         launch_diagnostics(g, st, s->XP, s->v, s->skeys, s->perm, s->cstart, s->cend,
                                             s->VX, n, OneScene{s->dc});
@@ -1202,7 +1208,7 @@ pbf_status pbf_find_cells(const uint32_t* sorted_keys, uint32_t n, uint32_t num_
     if (e == cudaSuccess && n > 0) {
         k_find_cells<<<grid_for(n), kBlock, 0, st>>>(sorted_keys, nullptr, nullptr, nullptr, n,
                                                      num_cells, start, end, bad, nullptr, nullptr,
-                                                     ScanPos{nullptr, nullptr}, nullptr);
+                                                     ScanPos{nullptr, nullptr}, nullptr, nullptr);
         e = cudaGetLastError();
     }
     uint32_t hbad = 0;

@@ -105,9 +105,19 @@ k_find_cells(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ pe
              const float4* __restrict__ xstar, float4* __restrict__ P0, uint32_t n, uint32_t ncells,
              int32_t* __restrict__ cstart, int32_t* __restrict__ cend, uint32_t* bad,
              const uint32_t* __restrict__ sid, uint32_t* __restrict__ sid_sorted, ScanPos sx,
-             uint32_t* __restrict__ runs) {
+             uint32_t* __restrict__ runs, uint32_t* status) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < n;
+    if (status) {
+        // neighbourcells.glsl:83 packs a 3-cell run's count into 8 bits
+        // (foreachneighbour.glsl:5 drops counts >= 128).  Particles i and
+        // i + 127 at most two cells apart in key order lie in one 3-cell
+        // window: flag it (conservatively: the window may span a row end).
+        const bool over = valid && i + 127u < n && skeys[i + 127u] - skeys[i] <= 2u;
+        if (__any_sync(0xFFFFFFFFu, over) && (threadIdx.x & 31u) == 0u &&
+            !(*(volatile uint32_t*)status & kDevRunOver127))
+            atomicOr(status, kDevRunOver127);
+    }
     float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (valid && P0) {
         p = __ldg(xstar + perm[i]);

@@ -14,7 +14,7 @@ __global__ void k_find_cells(const uint32_t* __restrict__ skeys, const uint32_t*
                              uint32_t ncells, int32_t* __restrict__ cstart,
                              int32_t* __restrict__ cend, uint32_t* bad,
                              const uint32_t* __restrict__ sid, uint32_t* __restrict__ sid_sorted,
-                             ScanPos sx, uint32_t* __restrict__ runs);
+                             ScanPos sx, uint32_t* __restrict__ runs, uint32_t* status);
 
 // Host launchers of the templated stage kernels (explicitly instantiated for
 // OneScene and ManyScenes in substep.cu).  The neighbour-sweep launchers take

@@ -319,6 +319,10 @@ class SPH:
     def kernels_per_substep(self) -> int:
         return int(self._lib.pbf_kernels_per_substep(self._h))
 
+    def kernels_launched(self) -> int:
+        """Kernels launched by this handle's substeps so far (pbf_kernels_launched)."""
+        return int(self._lib.pbf_kernels_launched(self._h))
+
     # ---- differentiation ------------------------------------------------------
     PARAM_NAMES = ("epsilon", "tensile_instability_k", "xsph_viscosity_c", "vorticity_epsilon")
 

@@ -301,8 +301,10 @@ def test_auto_is_the_default_and_resets(gpu):
     assert g.sweep_choice()["solver"] == "coop"
     g.set_tuning(auto_period=8)
     g.set_state(sc.x4, sc.v4)
+    l0 = g.kernels_launched()
     g.step(8)
     assert g.sweep_choice()["trials"] == 0
+    assert g.kernels_launched() - l0 == 8 * g.kernels_per_substep()
     g.step(4)  # the trial's substeps: one per candidate
     assert g.sweep_choice()["trials"] == 1
     g.set_state(sc.x4, sc.v4)

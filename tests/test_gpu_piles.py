@@ -42,6 +42,21 @@ def test_corner_piles_bit_exact(gpu, piled, tuning):
     x, v = g.get_state()
     assert_bits(x, ox, f"positions after {SUBSTEPS} substeps with {tuning}")
     assert_bits(v, ov, f"velocities after {SUBSTEPS} substeps with {tuning}")
+    # the reference's packed 8-bit run count (foreachneighbour.glsl:5) would
+    # have dropped these runs: the informational status bit says so
+    assert g.device_status() & pg.PBF_DEV_RUN_OVER_127
+
+
+def test_run_flag_clear_while_calm(gpu):
+    """Near rest density (8 particles per cell) no 3-cell run reaches 128:
+    the informational bit stays clear, so the packed form would agree (in
+    the oracle's sort the first window of 128 particles within three cells
+    appears at substep 25)."""
+    sc = scenes.plain_16k()
+    g = pg.SPH(sc.n, tuple(sc.params.grid), sc.params)
+    g.set_state(sc.x4, sc.v4)
+    g.step(10)
+    assert g.device_status() & pg.PBF_DEV_RUN_OVER_127 == 0
 
 
 def test_corner_piles_in_a_batch(gpu, oracle_mod):
