@@ -218,9 +218,9 @@ typedef struct pbf_tuning {
                                      warp-cooperative kernels, the rest a thread each
                                      (clumped states); 0 = off */
     uint32_t auto_period;         /* PBF_SWEEP_AUTO: substeps before the first trial and
-                                     between trials while the choice keeps changing
-                                     (doubling up to 256 substeps while it holds);
-                                     0 = 32 */
+                                     between trials while the choice or its measured
+                                     time keeps changing (doubling up to 256 substeps
+                                     while both hold); 0 = 32 */
 } pbf_tuning;
 
 /* PBF_SWEEP_AUTO (default): the solver sweeps (lambda + delta-p) and the two

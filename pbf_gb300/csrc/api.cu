@@ -192,16 +192,26 @@ void reset_sweep_choice(pbf_sim* s) {
     s->auto_next = s->auto_period;
     s->auto_trial = -1;
     s->auto_trials = 0;
+    s->auto_last_ms = 0.0;
+    for (uint32_t& k : s->auto_skip) k = 0;
 }
 
-// A trial's candidates: masked and direct always, the cooperative sweeps on
-// scenes small enough, and direct + cooperative once a pass has left the
-// masked configuration (in a calm state it costs ~2 substeps per trial).
+// A trial's candidates: masked and direct, the cooperative sweeps on scenes
+// small enough, and direct + cooperative once a pass has left the masked
+// configuration (in a calm state it costs ~2 substeps per trial).  A
+// configuration that took more than twice the best one's time sits out the
+// next 3 trials; the current choices always run.
 void pick_trial_candidates(pbf_sim* s) {
-    s->auto_cands = {PBF_PASS_MASKED, PBF_PASS_DIRECT};
-    if (s->n < kCoopTrialBelow) s->auto_cands.push_back(PBF_PASS_COOP);
+    std::vector<uint32_t> all = {PBF_PASS_MASKED, PBF_PASS_DIRECT};
+    if (s->n < kCoopTrialBelow) all.push_back(PBF_PASS_COOP);
     if (s->pass_solver != PBF_PASS_MASKED || s->pass_vort != PBF_PASS_MASKED)
-        s->auto_cands.push_back(PBF_PASS_DIRECT_COOP);
+        all.push_back(PBF_PASS_DIRECT_COOP);
+    s->auto_cands.clear();
+    for (uint32_t p : all) {
+        const bool current = p == s->pass_solver || p == s->pass_vort;
+        if (current || s->auto_skip[p] == 0) s->auto_cands.push_back(p);
+        else --s->auto_skip[p];
+    }
 }
 
 // SweepCfg modes (0 direct, 1 masked, 2 masked + pair lists, 3 cooperative)
@@ -413,7 +423,32 @@ pbf_status trial_substep(pbf_sim* s) {
     const uint32_t nv = s->params.vorticity_confinement
                             ? pick(s->pass_vort, 4 + 2 * (size_t)iters, 6 + 2 * (size_t)iters)
                             : s->pass_vort;
-    const bool changed = ns != s->pass_solver || nv != s->pass_vort;
+    // the chosen configurations' sweep time; a drift of more than 25% since
+    // the last trial means the state is still evolving: keep trials frequent
+    auto cand_of = [&](uint32_t pass) {
+        size_t c = 0;
+        while (c + 1 < nc && s->auto_cands[c] != pass) ++c;
+        return c;
+    };
+    double now_ms = span(cand_of(ns), 3, 3 + 2 * (size_t)iters);
+    if (s->params.vorticity_confinement)
+        now_ms += span(cand_of(nv), 4 + 2 * (size_t)iters, 6 + 2 * (size_t)iters);
+    const bool drifted = s->auto_last_ms > 0.0 &&
+                         (now_ms > 1.25 * s->auto_last_ms || now_ms < 0.8 * s->auto_last_ms);
+    s->auto_last_ms = now_ms;
+    {
+        auto total = [&](size_t c) {
+            double t = span(c, 3, 3 + 2 * (size_t)iters);
+            if (s->params.vorticity_confinement)
+                t += span(c, 4 + 2 * (size_t)iters, 6 + 2 * (size_t)iters);
+            return t;
+        };
+        double best = total(0);
+        for (size_t c = 1; c < nc; ++c) best = std::min(best, total(c));
+        for (size_t c = 0; c < nc; ++c)
+            if (total(c) > 2.0 * best) s->auto_skip[s->auto_cands[c]] = 3;
+    }
+    const bool changed = ns != s->pass_solver || nv != s->pass_vort || drifted;
     s->pass_solver = ns;
     s->pass_vort = nv;
     const uint32_t base = s->tuning.auto_period ? s->tuning.auto_period : kAutoPeriod;
@@ -695,6 +730,12 @@ pbf_status pbf_create_batch(const pbf_params* scene_params, const uint32_t* scen
     }
     s->stream = s->own_stream;
     reset_sweep_choice(s);
+    e = num_scenes == 1 ? preload_sweeps<OneScene>() : preload_sweeps<ManyScenes>();
+    if (e != cudaSuccess) {
+        pbf_status st = cuda_fail(nullptr, e, "pbf_create kernel load");
+        free_sim(s);
+        return st;
+    }
     s->sort.carve(s->sort_mem, n);
     e = cudaMemsetAsync(s->cstart, 0xFF, sizeof(int32_t) * s->ncells, s->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(s->cend, 0xFF, sizeof(int32_t) * s->ncells, s->stream);

@@ -1220,4 +1220,39 @@ void launch_diagnostics(unsigned g, cudaStream_t st, const float4* P, const floa
 PBF_INSTANTIATE(OneScene)
 PBF_INSTANTIATE(ManyScenes)
 
+// Loads every sweep kernel the automatic configuration may launch (the
+// runtime loads a kernel on its first use otherwise, a few hundred
+// microseconds each, which would land in the first trial's substeps).
+template <class CP>
+cudaError_t preload_sweeps() {
+    cudaFuncAttributes a;
+    cudaError_t e = cudaSuccess;
+    auto load = [&](const void* f) {
+        if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, f);
+    };
+    load((const void*)k_lambda_build<CP, kDirect, false>);
+    load((const void*)k_lambda_build<CP, kMasked, false>);
+    load((const void*)k_lambda_build<CP, kPairs, false>);
+    load((const void*)k_lambda<CP, kDirect, false>);
+    load((const void*)k_lambda<CP, kMasked, false>);
+    load((const void*)k_lambda<CP, kPairs, false>);
+    load((const void*)k_delta_p<CP, kDirect, false>);
+    load((const void*)k_delta_p<CP, kMasked, false>);
+    load((const void*)k_delta_p<CP, kPairs, false>);
+    load((const void*)k_vorticity_a<CP, kDirect, false>);
+    load((const void*)k_vorticity_a<CP, kMasked, false>);
+    load((const void*)k_vorticity_a<CP, kPairs, false>);
+    load((const void*)k_vorticity_b<CP, kDirect, false>);
+    load((const void*)k_vorticity_b<CP, kMasked, false>);
+    load((const void*)k_vorticity_b<CP, kPairs, false>);
+    load((const void*)k_lambda_coop<CP>);
+    load((const void*)k_delta_p_coop<CP>);
+    load((const void*)k_vorticity_a_coop<CP>);
+    load((const void*)k_vorticity_b_coop<CP>);
+    load((const void*)k_run_flags);
+    return e;
+}
+template cudaError_t preload_sweeps<OneScene>();
+template cudaError_t preload_sweeps<ManyScenes>();
+
 }  // namespace pbf

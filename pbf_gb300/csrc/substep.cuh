@@ -50,6 +50,9 @@ void launch_delta_p(SweepCfg sw, cudaStream_t st, const float4* L, const float4*
                     const uint32_t* skeys, const int32_t* cstart, const int32_t* cend, float4* Pn,
                     NbrLists nl, PairLists pr, ScanPos sx, ScanPos sx_out, int dmax_slot,
                     int out_slot, uint32_t n, CP cp, uint32_t* status);
+// Loads the sweep kernels the automatic configuration may launch.
+template <class CP>
+cudaError_t preload_sweeps();
 template <class CP>
 void launch_heavy_scan(unsigned g, cudaStream_t st, const uint32_t* skeys, const int32_t* cstart,
                        const int32_t* cend, uint32_t threshold, uint32_t n, CP cp, uint8_t* heavy,
