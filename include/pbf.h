@@ -236,7 +236,8 @@ enum {
     PBF_PASS_DIRECT = 1,      /* direct stencil loops */
     PBF_PASS_COOP = 2,        /* warp-cooperative sweeps */
     PBF_PASS_DIRECT_COOP = 3  /* direct first sweep (lambda, vorticity a), cooperative second
-                                 (delta-p, vorticity b) */
+                                 (delta-p, vorticity b); not among the automatic mode's
+                                 candidates (its cooperative sweeps walk piles pair by pair) */
 };
 
 /* No reference counterpart (the reference has no tuning surface). */

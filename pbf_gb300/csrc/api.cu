@@ -196,16 +196,15 @@ void reset_sweep_choice(pbf_sim* s) {
     for (uint32_t& k : s->auto_skip) k = 0;
 }
 
-// A trial's candidates: masked and direct, the cooperative sweeps on scenes
-// small enough, and direct + cooperative once a pass has left the masked
-// configuration (in a calm state it costs ~2 substeps per trial).  A
+// A trial's candidates: masked and direct, and the cooperative sweeps on
+// scenes small enough.  (Direct + cooperative is not tried: its cooperative
+// second sweep has no run path, so it wins while piles are small and then
+// costs O(pile^2 / 32) as they grow, where the direct sweeps stay fast.)  A
 // configuration that took more than twice the best one's time sits out the
 // next 3 trials; the current choices always run.
 void pick_trial_candidates(pbf_sim* s) {
     std::vector<uint32_t> all = {PBF_PASS_MASKED, PBF_PASS_DIRECT};
     if (s->n < kCoopTrialBelow) all.push_back(PBF_PASS_COOP);
-    if (s->pass_solver != PBF_PASS_MASKED || s->pass_vort != PBF_PASS_MASKED)
-        all.push_back(PBF_PASS_DIRECT_COOP);
     s->auto_cands.clear();
     for (uint32_t p : all) {
         const bool current = p == s->pass_solver || p == s->pass_vort;

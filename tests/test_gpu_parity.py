@@ -272,9 +272,9 @@ def test_tuning_never_changes_results(gpu, oracle_mod, tuning):
 def test_auto_sweeps_never_change_results(gpu, oracle_mod, extra):
     """PBF_SWEEP_AUTO with a trial every few substeps: each trial steps one
     real substep under each candidate configuration of the solver and
-    vorticity passes (masked, direct, cooperative, direct + cooperative), so
-    every configuration and every switch between them runs inside these 30
-    substeps, and the result is the oracle's bits."""
+    vorticity passes (masked, direct, cooperative), so every configuration
+    and every switch between them runs inside these 30 substeps, and the
+    result is the oracle's bits."""
     sc = scenes.plain_16k()
     g = pg.SPH(sc.n, tuple(sc.params.grid), sc.params)
     g.set_tuning(sweep_mode="auto", auto_period=2, **extra)
