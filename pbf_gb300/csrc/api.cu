@@ -194,6 +194,7 @@ void reset_sweep_choice(pbf_sim* s) {
     s->auto_trials = 0;
     s->auto_last_ms = 0.0;
     for (uint32_t& k : s->auto_skip) k = 0;
+    for (uint32_t& k : s->auto_skip_len) k = 0;
 }
 
 // A trial's candidates: masked and direct, and the cooperative sweeps on
@@ -201,7 +202,8 @@ void reset_sweep_choice(pbf_sim* s) {
 // second sweep has no run path, so it wins while piles are small and then
 // costs O(pile^2 / 32) as they grow, where the direct sweeps stay fast.)  A
 // configuration that took more than twice the best one's time sits out the
-// next 3 trials; the current choices always run.
+// next 3 trials, twice as many each time it loses that way again (up to 64);
+// the current choices always run.
 void pick_trial_candidates(pbf_sim* s) {
     std::vector<uint32_t> all = {PBF_PASS_MASKED, PBF_PASS_DIRECT};
     if (s->n < kCoopTrialBelow) all.push_back(PBF_PASS_COOP);
@@ -444,8 +446,15 @@ pbf_status trial_substep(pbf_sim* s) {
         };
         double best = total(0);
         for (size_t c = 1; c < nc; ++c) best = std::min(best, total(c));
-        for (size_t c = 0; c < nc; ++c)
-            if (total(c) > 2.0 * best) s->auto_skip[s->auto_cands[c]] = 3;
+        for (size_t c = 0; c < nc; ++c) {
+            uint32_t& len = s->auto_skip_len[s->auto_cands[c]];
+            if (total(c) > 2.0 * best) {
+                len = len ? std::min(2 * len, 64u) : 3u;
+                s->auto_skip[s->auto_cands[c]] = len;
+            } else {
+                len = 0;
+            }
+        }
     }
     const bool changed = ns != s->pass_solver || nv != s->pass_vort || drifted;
     s->pass_solver = ns;

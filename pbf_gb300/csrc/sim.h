@@ -85,7 +85,8 @@ struct pbf_sim {
     int auto_trial = -1;
     uint32_t auto_trials = 0;
     double auto_last_ms = 0.0;  // sweep time of the chosen configurations at the last trial
-    uint32_t auto_skip[4] = {};  // trials a configuration sits out (it was > 2x the best)
+    uint32_t auto_skip[4] = {};      // trials a configuration sits out (it was > 2x the best)
+    uint32_t auto_skip_len[4] = {};  // its last sit-out (doubles while it keeps losing)
     uint64_t launched = 0;  // kernels launched by substeps so far (pbf_kernels_launched)
     std::vector<uint32_t> auto_cands;
     std::vector<cudaEvent_t> trial_ev;  // (7 + 2 * iterations) per candidate
