@@ -166,13 +166,6 @@ pbf_tuning default_tuning(uint32_t n) {
     return t;
 }
 
-// PBF_SWEEP_AUTO: substeps before the first trial and between trials while
-// the choice changes; the period doubles up to kAutoPeriodMax while it holds.
-// A candidate replaces the current configuration only if it was at least 3%
-// faster in the trial (the state drifts between the trial's substeps).
-constexpr uint32_t kAutoPeriod = 32;
-constexpr uint32_t kAutoPeriodMax = 256;
-constexpr double kAutoMargin = 0.97;
 // The all-cooperative candidate is tried below this many particles only: a
 // warp per particle costs ~3x the instructions and, on a GPU that a thread per
 // particle already fills, a trial substep under it costs several substeps.
@@ -187,32 +180,16 @@ void reset_sweep_choice(pbf_sim* s) {
                                           : PBF_PASS_MASKED;
     if (m == PBF_SWEEP_AUTO) pass = s->n < kCoopBelow ? PBF_PASS_COOP : PBF_PASS_MASKED;
     s->pass_solver = s->pass_vort = pass;
-    s->auto_period = s->tuning.auto_period ? s->tuning.auto_period : kAutoPeriod;
-    s->auto_count = 0;
-    s->auto_next = s->auto_period;
+    s->autop.reset(s->tuning.auto_period);
     s->auto_trial = -1;
-    s->auto_trials = 0;
-    s->auto_last_ms = 0.0;
-    for (uint32_t& k : s->auto_skip) k = 0;
-    for (uint32_t& k : s->auto_skip_len) k = 0;
 }
 
-// A trial's candidates: masked and direct, and the cooperative sweeps on
-// scenes small enough.  (Direct + cooperative is not tried: its cooperative
-// second sweep has no run path, so it wins while piles are small and then
-// costs O(pile^2 / 32) as they grow, where the direct sweeps stay fast.)  A
-// configuration that took more than twice the best one's time sits out the
-// next 3 trials, twice as many each time it loses that way again (up to 64);
-// the current choices always run.
+// A trial's candidates (auto_policy.h).  (Direct + cooperative is not tried:
+// its cooperative second sweep has no run path, so it wins while piles are
+// small and then costs O(pile^2 / 32) as they grow, where the direct sweeps
+// stay fast.)
 void pick_trial_candidates(pbf_sim* s) {
-    std::vector<uint32_t> all = {PBF_PASS_MASKED, PBF_PASS_DIRECT};
-    if (s->n < kCoopTrialBelow) all.push_back(PBF_PASS_COOP);
-    s->auto_cands.clear();
-    for (uint32_t p : all) {
-        const bool current = p == s->pass_solver || p == s->pass_vort;
-        if (current || s->auto_skip[p] == 0) s->auto_cands.push_back(p);
-        else --s->auto_skip[p];
-    }
+    s->auto_cands = s->autop.candidates(s->pass_solver, s->pass_vort, s->n < kCoopTrialBelow);
 }
 
 // SweepCfg modes (0 direct, 1 masked, 2 masked + pair lists, 3 cooperative)
@@ -384,9 +361,8 @@ pbf_status launch_graph(pbf_sim* s, uint32_t count) {
 
 // One substep of a PBF_SWEEP_AUTO trial: the next candidate configuration for
 // both passes, eager, with stage events.  After the last candidate, waits for
-// the trial's events and keeps, for the solver sweeps and for the vorticity
-// passes separately, the fastest configuration (a candidate must beat the
-// current one by kAutoMargin).  The period doubles while the choice holds.
+// the trial's events and hands each candidate's solver and vorticity times
+// to the policy (auto_policy.h), which keeps the choices and the schedule.
 pbf_status trial_substep(pbf_sim* s) {
     NvtxRange nvtx_("sweep trial substep");
     const uint32_t iters = s->params.num_solver_iterations;
@@ -412,58 +388,14 @@ pbf_status trial_substep(pbf_sim* s) {
         cudaEventElapsedTime(&m, s->trial_ev[per * c + a], s->trial_ev[per * c + b]);
         return (double)m;
     };
-    auto pick = [&](uint32_t cur, size_t a, size_t b) {
-        size_t best = 0, at_cur = 0;
-        for (size_t c = 0; c < nc; ++c) {
-            if (span(c, a, b) < span(best, a, b)) best = c;
-            if (s->auto_cands[c] == cur) at_cur = c;
-        }
-        return span(best, a, b) < kAutoMargin * span(at_cur, a, b) ? s->auto_cands[best] : cur;
-    };
-    const uint32_t ns = pick(s->pass_solver, 3, 3 + 2 * (size_t)iters);
-    const uint32_t nv = s->params.vorticity_confinement
-                            ? pick(s->pass_vort, 4 + 2 * (size_t)iters, 6 + 2 * (size_t)iters)
-                            : s->pass_vort;
-    // the chosen configurations' sweep time; a drift of more than 25% since
-    // the last trial means the state is still evolving: keep trials frequent
-    auto cand_of = [&](uint32_t pass) {
-        size_t c = 0;
-        while (c + 1 < nc && s->auto_cands[c] != pass) ++c;
-        return c;
-    };
-    double now_ms = span(cand_of(ns), 3, 3 + 2 * (size_t)iters);
-    if (s->params.vorticity_confinement)
-        now_ms += span(cand_of(nv), 4 + 2 * (size_t)iters, 6 + 2 * (size_t)iters);
-    const bool drifted = s->auto_last_ms > 0.0 &&
-                         (now_ms > 1.25 * s->auto_last_ms || now_ms < 0.8 * s->auto_last_ms);
-    s->auto_last_ms = now_ms;
-    {
-        auto total = [&](size_t c) {
-            double t = span(c, 3, 3 + 2 * (size_t)iters);
-            if (s->params.vorticity_confinement)
-                t += span(c, 4 + 2 * (size_t)iters, 6 + 2 * (size_t)iters);
-            return t;
-        };
-        double best = total(0);
-        for (size_t c = 1; c < nc; ++c) best = std::min(best, total(c));
-        for (size_t c = 0; c < nc; ++c) {
-            uint32_t& len = s->auto_skip_len[s->auto_cands[c]];
-            if (total(c) > 2.0 * best) {
-                len = len ? std::min(2 * len, 64u) : 3u;
-                s->auto_skip[s->auto_cands[c]] = len;
-            } else {
-                len = 0;
-            }
-        }
+    std::vector<double> solver_ms(nc), vort_ms(nc);
+    for (size_t c = 0; c < nc; ++c) {
+        solver_ms[c] = span(c, 3, 3 + 2 * (size_t)iters);
+        vort_ms[c] = span(c, 4 + 2 * (size_t)iters, 6 + 2 * (size_t)iters);
     }
-    const bool changed = ns != s->pass_solver || nv != s->pass_vort || drifted;
-    s->pass_solver = ns;
-    s->pass_vort = nv;
-    const uint32_t base = s->tuning.auto_period ? s->tuning.auto_period : kAutoPeriod;
-    s->auto_period = changed ? base : std::min(2 * s->auto_period, std::max(base, kAutoPeriodMax));
-    s->auto_next = s->auto_count + 1 + s->auto_period;  // counted after this substep
+    s->autop.finish(s->auto_cands, solver_ms.data(), vort_ms.data(),
+                    s->params.vorticity_confinement != 0, s->pass_solver, s->pass_vort);
     s->auto_trial = -1;
-    s->auto_trials++;
     return PBF_OK;
 }
 
@@ -1028,7 +960,7 @@ pbf_status pbf_step(pbf_sim* s, uint32_t substeps) {
     const bool autom = s->tuning.sweep_mode == PBF_SWEEP_AUTO;
     uint32_t left = substeps;
     while (left > 0) {
-        if (autom && s->auto_trial < 0 && s->auto_count >= s->auto_next) {
+        if (autom && s->auto_trial < 0 && s->autop.trial_due()) {
             pick_trial_candidates(s);
             s->auto_trial = 0;
         }
@@ -1036,15 +968,15 @@ pbf_status pbf_step(pbf_sim* s, uint32_t substeps) {
             pbf_status r = trial_substep(s);
             if (r != PBF_OK) return r;
             --left;
-            ++s->auto_count;
+            ++s->autop.count;
             continue;
         }
         uint32_t run = left;
-        if (autom) run = (uint32_t)std::min<uint64_t>(left, s->auto_next - s->auto_count);
+        if (autom) run = (uint32_t)std::min<uint64_t>(left, s->autop.next - s->autop.count);
         pbf_status r = launch_graph(s, run);
         if (r != PBF_OK) return r;
         left -= run;
-        s->auto_count += run;
+        s->autop.count += run;
     }
     return PBF_OK;
 }
@@ -1053,7 +985,7 @@ pbf_status pbf_get_sweep_choice(const pbf_sim* s, uint32_t out[3]) {
     if (!s || !out) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "NULL argument");
     out[0] = s->pass_solver;
     out[1] = s->pass_vort;
-    out[2] = s->auto_trials;
+    out[2] = s->autop.trials;
     return PBF_OK;
 }
 

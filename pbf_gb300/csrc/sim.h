@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "../../include/pbf.h"
+#include "auto_policy.h"
 #include "common.cuh"
 #include "sort.cuh"
 
@@ -77,19 +78,14 @@ struct pbf_sim {
     cudaGraph_t graphs[16] = {};
     cudaGraphExec_t execs[16] = {};
 
-    // PBF_SWEEP_AUTO: substeps since the last reset, substep of the next
-    // trial, current trial period, candidate the running trial steps next
-    // (-1: none), trials so far, the trial's candidates and their events
-    uint64_t auto_count = 0, auto_next = 0;
-    uint32_t auto_period = 0;
+    // PBF_SWEEP_AUTO: the schedule and sit-outs (auto_policy.h), the
+    // candidate the running trial steps next (-1: none), the trial's
+    // candidates and their stage events
+    pbf::AutoPolicy autop;
     int auto_trial = -1;
-    uint32_t auto_trials = 0;
-    double auto_last_ms = 0.0;  // sweep time of the chosen configurations at the last trial
-    uint32_t auto_skip[4] = {};      // trials a configuration sits out (it was > 2x the best)
-    uint32_t auto_skip_len[4] = {};  // its last sit-out (doubles while it keeps losing)
-    uint64_t launched = 0;  // kernels launched by substeps so far (pbf_kernels_launched)
     std::vector<uint32_t> auto_cands;
     std::vector<cudaEvent_t> trial_ev;  // (7 + 2 * iterations) per candidate
+    uint64_t launched = 0;  // kernels launched by substeps so far (pbf_kernels_launched)
 
     bool timing = false;
     std::vector<cudaEvent_t> ev;  // 7 + 2 * iterations stage boundaries
