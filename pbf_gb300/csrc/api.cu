@@ -148,13 +148,13 @@ constexpr uint32_t kCoopBelow = 32768;
 
 // The autotuner's mixed-sweep candidate: warps for particles with more than
 // 256 stencil candidates (in the dam break's initial lattice, 8 particles
-// per cell, an interior particle has 216).  It wins
-// while the fluid is part clumped (262,144 particles: 2.7 ms per substep
-// against 4.2 cooperative and 5.7 masked) and loses once every particle is
-// over the threshold, so it is not a default.
+// per cell, an interior particle has 216).  It won while the fluid was part
+// clumped (262,144 particles: 2.7 ms per substep against 4.2 cooperative and
+// 5.7 masked, before the direct sweeps skipped pile runs) and loses once
+// every particle is over the threshold, so it is not a default.
 constexpr uint32_t kMixedCandidates = 256;
 
-pbf_tuning default_tuning(uint32_t n) {
+pbf_tuning default_tuning() {
     pbf_tuning t{};
     t.use_neighbour_lists = 0;
     t.list_capacity = 128;
@@ -162,7 +162,6 @@ pbf_tuning default_tuning(uint32_t n) {
     t.block_size = 256;
     t.sweep_mode = PBF_SWEEP_AUTO;
     t.pair_list_capacity = 128;
-    (void)n;
     return t;
 }
 
@@ -630,7 +629,7 @@ pbf_status pbf_create_batch(const pbf_params* scene_params, const uint32_t* scen
     s->sparams.assign(scene_params, scene_params + num_scenes);
     s->counts.assign(scene_counts, scene_counts + num_scenes);
     s->params = scene_params[0];
-    s->tuning = default_tuning(n);
+    s->tuning = default_tuning();
     s->n = n;
     s->ncells = (uint32_t)cells;
     s->numbits = sort_numbits_for_cells(s->ncells);
