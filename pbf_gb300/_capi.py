@@ -26,6 +26,16 @@ PBF_DEV_RUN_OVER_127 = 0x4
 PBF_HOST = 0
 PBF_DEVICE = 1
 
+PBF_SWEEP_DIRECT = 0
+PBF_SWEEP_MASKED = 1
+PBF_SWEEP_COOP = 2
+PBF_SWEEP_AUTO = 3
+
+PBF_PASS_MASKED = 0
+PBF_PASS_DIRECT = 1
+PBF_PASS_COOP = 2
+PBF_PASS_DIRECT_COOP = 3
+
 
 class Params(C.Structure):
     """pbf_params (include/pbf.h)."""

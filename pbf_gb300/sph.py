@@ -18,6 +18,7 @@ import ctypes as C
 
 import numpy as np
 
+from . import _capi
 from ._capi import (PBF_DEVICE, PBF_HOST, Diagnostics, ParamGrads, Params, PbfError, Tuning,
                     check, load)
 
@@ -181,7 +182,9 @@ class SPH:
         if block_size is not None:
             t.block_size = int(block_size)
         if sweep_mode is not None:
-            t.sweep_mode = {"direct": 0, "masked": 1, "coop": 2, "auto": 3}.get(sweep_mode, sweep_mode)
+            t.sweep_mode = {"direct": _capi.PBF_SWEEP_DIRECT, "masked": _capi.PBF_SWEEP_MASKED,
+                            "coop": _capi.PBF_SWEEP_COOP,
+                            "auto": _capi.PBF_SWEEP_AUTO}.get(sweep_mode, sweep_mode)
         if pair_list_capacity is not None:
             t.pair_list_capacity = int(pair_list_capacity)
         if coop_candidates is not None:

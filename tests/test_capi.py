@@ -134,3 +134,26 @@ def test_struct_mirrors_match_header(tmp_path):
         assert C.sizeof(st) == got[(cname, "size")], f"{py} size"
         for field, _ in st._fields_:
             assert getattr(st, field).offset == got[(cname, field)], f"{py}.{field} offset"
+
+
+def test_header_constants_match_python():
+    """Every PBF_* constant include/pbf.h defines (macros and enumerators)
+    has the same value in the Python binding, which mirrors all of them
+    (pbf_gb300._capi; the splat pass numbers in pbf_gb300.splat)."""
+    import re
+    from pbf_gb300 import splat
+    text = open(os.path.join(ROOT, "include", "pbf.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    consts = {}
+    for name, val in re.findall(r"^#define (PBF_\w+) (0x[0-9a-fA-F]+|\d+)u?\s*$", text, flags=re.M):
+        consts[name] = int(val, 0)
+    for body in re.findall(r"enum\s*\w*\s*\{(.*?)\}", text, flags=re.S):
+        for name, val in re.findall(r"(PBF_\w+)\s*=\s*(\d+)", body):
+            consts[name] = int(val)
+    consts.pop("PBF_ABI_VERSION", None)  # checked by test_abi_version_and_status_strings
+    assert len(consts) >= 20
+    alias = {"PBF_SPLAT_DEPTH": (splat, "DEPTH"), "PBF_SPLAT_THICKNESS": (splat, "THICKNESS")}
+    for name, val in consts.items():
+        mod, attr = alias.get(name, (_capi, name))
+        assert hasattr(mod, attr), f"{name} is not mirrored in Python"
+        assert getattr(mod, attr) == val, f"{name}: header {val}, Python {getattr(mod, attr)}"
