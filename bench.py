@@ -510,6 +510,12 @@ def main():
         if rank == 0:
             print(json.dumps(reference_arm(args, scene)), flush=True)
         return 0
+    if world > 1:
+        # replicas: the window and e2e lines scale; the single-GPU legs
+        # (full runs, batch, adjoint, splatting, the 16k configuration) would
+        # only repeat on every rank
+        args.no_stable = args.no_full = args.no_batched = args.no_adjoint = True
+        args.no_splat = args.no_small = True
 
     import torch
     import torch.distributed as dist
