@@ -174,7 +174,9 @@ pbf_status pbf_device_buffers(pbf_sim* sim, float** x4, float** v4);
  * x (lambda, delta-p + wall clamp), velocity commit, and, when
  * vorticity_confinement is set, XSPH viscosity + vorticity confinement.
  * Asynchronous on the handle's stream.  After the first call the substep is
- * replayed from a captured CUDA graph. */
+ * replayed from a captured CUDA graph (one per sweep configuration).  Under
+ * PBF_SWEEP_AUTO, a call in which a trial completes waits on the host for the
+ * trial's substeps (at most once per trial period, 32 to 256 substeps). */
 pbf_status pbf_step(pbf_sim* sim, uint32_t substeps);
 
 /* Performance knobs of a handle.  None of them changes any result: every
