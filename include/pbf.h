@@ -36,7 +36,10 @@
 extern "C" {
 #endif
 
-#define PBF_ABI_VERSION 1
+/* Bumped whenever a struct passed across the ABI changes layout (2: pbf_tuning
+ * gained coop_candidates and auto_period).  A caller compiled against another
+ * version must not pass its structs to this library. */
+#define PBF_ABI_VERSION 2
 
 typedef enum pbf_status {
     PBF_OK = 0,
@@ -439,6 +442,7 @@ void pbf_debug_fail_allocation(int after);
 /* Message of the last failed call on `sim`, or of the last failed call
  * without a handle when sim is NULL.  Never NULL. */
 const char* pbf_last_error(const pbf_sim* sim);
+/* PBF_ABI_VERSION of the built library. */
 int pbf_abi_version(void);
 
 #ifdef __cplusplus

@@ -32,7 +32,11 @@ def test_every_declared_symbol_is_exported(product_lib):
 
 
 def test_abi_version_and_status_strings(product_lib):
-    assert product_lib.pbf_abi_version() == 1
+    import re
+    text = open(os.path.join(ROOT, "include", "pbf.h")).read()
+    header = int(re.search(r"#define PBF_ABI_VERSION (\d+)", text).group(1))
+    assert header == 2
+    assert product_lib.pbf_abi_version() == header
     assert product_lib.pbf_status_string(0) == b"ok"
     assert product_lib.pbf_status_string(1) == b"invalid argument"
 
