@@ -315,6 +315,7 @@ pbf_status pbf_get_solver(pbf_sim* sim, float* lambda_sorted, float* xpred4_sort
  * of n 32-bit keys on their low `numbits` bits (1..32), onesweep with
  * decoupled lookback.  perm_out[i] = input index of the i-th smallest key,
  * ties in input order; keys_out (may be NULL) receives the sorted keys.
+ * keys_out and perm_out must not alias keys_in or each other.
  * Device pointers; runs on `stream` and synchronises before returning.
  * Scratch memory is allocated by the library on first use and cached. */
 pbf_status pbf_radix_sort(const uint32_t* keys_in, uint32_t* keys_out, uint32_t* perm_out,
@@ -323,17 +324,21 @@ pbf_status pbf_radix_sort(const uint32_t* keys_in, uint32_t* keys_out, uint32_t*
 /* Allocation-free variant of pbf_radix_sort, with the same arguments and
  * results.  No counterpart in the reference (its RadixSort allocates its GL
  * buffers in the constructor, where allocation is always allowed).  For
- * callers that cannot call cudaMalloc: code running inside CUDA graph
- * capture, a host application whose allocator owns all device memory, or a
- * real-time loop that must not block on the allocator.  It allocates
+ * callers that cannot call cudaMalloc: a host application whose own
+ * allocator has reserved all of the GPU's memory (a cudaMalloc from this
+ * library would fail or steal from its pool), or a real-time loop that must
+ * not stall on the allocator's implicit synchronisation.  It allocates
  * nothing: its scratch is one device array inside the library, sized for at
  * most 1,048,576 keys (larger n returns PBF_ERR_INVALID_ARGUMENT), which every
  * GPU that loads the library holds (about 13.6 MB) until the process exits.
- * The first call on a device looks up that array's device address; make the
- * first call on each device before any stream capture.  All calls share the
- * array, so calls whose work overlaps on the GPU (other streams, other host
- * threads) race and corrupt each other: serialise them.  Device pointers;
- * runs on `stream` and synchronises before returning. */
+ * The first call on a device looks up that array's device address (once per
+ * device, cached for the life of the process, so cudaDeviceReset after it is
+ * not supported); make the first call on each device before any stream
+ * capture.  All calls share the array, and each call clears what must start
+ * at zero; calls whose work overlaps on the GPU (other streams, other host
+ * threads) race and corrupt each other: serialise them.  keys_out and
+ * perm_out must not alias keys_in or each other.  Device pointers; runs on
+ * `stream` and synchronises before returning. */
 pbf_status pbf_radix_sort_noalloc(const uint32_t* keys_in, uint32_t* keys_out, uint32_t* perm_out,
                                   uint32_t n, uint32_t numbits, void* stream);
 

@@ -18,8 +18,7 @@
 //   constants          src/SPH.cpp:28-60,136-144,159-164
 // in FP32 (T = float) and as an FP64 twin (T = double) from one template.
 //
-// Decisions on the reference's undefined or buggy behaviour (all documented
-// in oracle/README.md):
+// Decisions on the reference's undefined or buggy behaviour:
 //   Q1  h is a parameter; the stencil is the 27 cells around the particle's
 //       cell as in the reference, so h <= 1 makes it complete.
 //   Q2  cell coordinate = min(int(clamp(x, 0, G)), G - 1) per axis, used for

@@ -9,7 +9,7 @@
 // velocity image and the vorticity buffer it also reads, vorticity.glsl:50,
 // 60-72, 85), each invocation's own write is held back until the dispatch
 // ends, so every read sees the dispatch's input: the Jacobi reading of the
-// reference's acknowledged races (decision Q5 of oracle/README.md).  The
+// reference's acknowledged races (decision Q5: Jacobi order).  The
 // vorticity shader's barrier() is honoured by running the dispatch twice: the
 // first pass fills the vorticity buffer (phase one of every invocation), the
 // second pass reads it complete.

@@ -1139,6 +1139,13 @@ pbf_status pbf_radix_sort(const uint32_t* keys_in, uint32_t* keys_out, uint32_t*
     if (!keys_in || !perm_out) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "keys_in and perm_out are required");
     if (n >= (1u << 30)) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "n must be below 2^30");
     if (numbits < 1 || numbits > 32) return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "numbits must be in [1, 32]");
+    // The sort reads its key buffer once per pass and writes keys and ids in
+    // the same final pass: no output may alias keys_in or the other output.
+    if ((const void*)perm_out == (const void*)keys_in ||
+        (keys_out && (const void*)keys_out == (const void*)keys_in))
+        return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "outputs must not alias keys_in");
+    if (keys_out && (const void*)keys_out == (const void*)perm_out)
+        return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "keys_out must not alias perm_out");
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return fail(nullptr, PBF_ERR_NO_DEVICE, "no CUDA device");
     cudaStream_t st = (cudaStream_t)stream;
@@ -1160,10 +1167,7 @@ pbf_status pbf_radix_sort(const uint32_t* keys_in, uint32_t* keys_out, uint32_t*
         c.keys_scratch = (uint32_t*)((uint8_t*)c.mem + wsb);
         c.status = (uint32_t*)((uint8_t*)c.keys_scratch + sizeof(uint32_t) * (size_t)n);
     }
-    // The sort reads its key buffer once per pass; keys_out must not alias keys_in.
     uint32_t* kout = keys_out ? keys_out : c.keys_scratch;
-    if ((const void*)kout == (const void*)keys_in || (const void*)perm_out == (const void*)keys_in)
-        return fail(nullptr, PBF_ERR_INVALID_ARGUMENT, "outputs must not alias keys_in");
     cudaError_t e = cudaMemsetAsync(c.status, 0, sizeof(uint32_t), st);
     if (e == cudaSuccess) e = sort_pairs(c.ws, keys_in, kout, perm_out, n, numbits, c.status, st);
     uint32_t bits = 0;

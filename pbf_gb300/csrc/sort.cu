@@ -286,9 +286,10 @@ cudaError_t sort_pairs(const SortWorkspace& ws, const uint32_t* keys_in, uint32_
 // ---- allocation-free variant -------------------------------------------------
 //
 // For callers that must not allocate device memory: a library embedded in a
-// host application whose allocator owns all of the GPU's memory, code that
-// runs while a CUDA graph is being captured (where cudaMalloc is not
-// allowed), or a real-time loop that may not block on the allocator.  The
+// host application whose own allocator has reserved all of the GPU's memory
+// (a cudaMalloc here would fail or take memory from its pool), or a
+// real-time loop that may not stall on the allocator's implicit
+// synchronisation.  The
 // sort's scratch (digit histograms, lookback status, ping-pong buffers, a key
 // buffer for callers that want no sorted keys, the status word) lives in one
 // file-scope device array sized for at most kNoAllocMaxKeys keys.  Every GPU
@@ -304,7 +305,9 @@ static constexpr int kNoAllocMaxDevices = 64;
 static __device__ __align__(256) uint8_t g_sort_scratch[kNoAllocBytes];
 
 // Host code cannot use g_sort_scratch's name as a device address; the address
-// is looked up once per device (with that device current) and cached.
+// is looked up once per device (with that device current) and cached for the
+// life of the process, so a cudaDeviceReset after the first call on a device
+// is not supported (the module would be reloaded at another address).
 static std::mutex g_sort_scratch_mu;
 static void* g_sort_scratch_addr[kNoAllocMaxDevices] = {};
 
@@ -341,6 +344,8 @@ extern "C" pbf_status pbf_radix_sort_noalloc(const uint32_t* keys_in, uint32_t* 
     if ((const void*)perm_out == (const void*)keys_in ||
         (keys_out && (const void*)keys_out == (const void*)keys_in))
         return noalloc_fail(PBF_ERR_INVALID_ARGUMENT, "outputs must not alias keys_in");
+    if (keys_out && (const void*)keys_out == (const void*)perm_out)
+        return noalloc_fail(PBF_ERR_INVALID_ARGUMENT, "keys_out must not alias perm_out");
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) {
         cudaGetLastError();

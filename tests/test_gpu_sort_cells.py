@@ -63,6 +63,11 @@ def test_radix_sort_empty_and_errors(gpu):
     p = torch.zeros(8, dtype=torch.int32, device="cuda")
     assert gpu.pbf_radix_sort(k.data_ptr(), None, p.data_ptr(), 8, 0, None) == 1
     assert gpu.pbf_radix_sort(k.data_ptr(), None, p.data_ptr(), 8, 33, None) == 1
+    q = torch.zeros(8, dtype=torch.int32, device="cuda")
+    # keys_out aliasing perm_out would make the final pass overwrite one with the other
+    for fn in (gpu.pbf_radix_sort, gpu.pbf_radix_sort_noalloc):
+        assert fn(k.data_ptr(), q.data_ptr(), q.data_ptr(), 8, 8, None) == 1
+        assert fn(k.data_ptr(), k.data_ptr(), q.data_ptr(), 8, 8, None) == 1
 
 
 def ref_cells(sorted_keys, ncells):

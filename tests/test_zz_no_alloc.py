@@ -1,9 +1,9 @@
 """The allocation-free radix sort, pbf_radix_sort_noalloc, through the C ABI.
 
-Some callers cannot allocate device memory while they sort: code running
-inside CUDA graph capture (cudaMalloc is not allowed there), a host
-application whose own allocator owns all of the GPU's memory, or a real-time
-loop that must not block on the allocator.  The variant keeps its scratch in
+Some callers cannot allocate device memory while they sort: a host
+application whose own allocator has reserved all of the GPU's memory (a
+cudaMalloc from the library would fail or take from its pool), or a
+real-time loop that must not stall on the allocator.  The variant keeps its scratch in
 one device array inside the library (at most 1,048,576 keys), so it must give
 exactly what the allocating entry point gives, also on a second call right
 after a first one that left the shared array full of another sort's state.
