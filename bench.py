@@ -74,7 +74,9 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true",
                     help="the default (kept for older command lines)")
     ap.add_argument("--recovery", action="store_true",
-                    help="also run the 64-scene parameter recovery (about a minute)")
+                    help="the default (kept for older command lines)")
+    ap.add_argument("--no-recovery", action="store_true",
+                    help="skip the 64-scene parameter recovery (about a minute)")
     return ap.parse_args()
 
 
@@ -445,9 +447,12 @@ def small_config(stream, with_cpu: bool):
     return res
 
 
-def cpu_baseline(scene, substeps: int):
-    """FP32 oracle on all host threads, `substeps` full substeps of the scene."""
+def cpu_baseline(scene_name: str, substeps: int):
+    """FP32 oracle on all host threads, `substeps` full substeps of the scene
+    (built by the oracle's own generator)."""
     import oracle
+    from oracle import scenes as oscenes
+    scene = getattr(oscenes, scene_name)()
     o = oracle.Oracle(scene.params, scene.n)
     o.set_state(scene.x4, scene.v4)
     secs = o.step(substeps)
@@ -458,64 +463,117 @@ def cpu_baseline(scene, substeps: int):
                       f"initial state ({secs:.1f} s, FP32 oracle, OpenMP)"}
 
 
-def reference_arm(args, scene):
-    """The reference path's CPU implementation (the oracle port) on the host."""
+def workload_config(scene, K: int, world: int) -> dict:
+    """The `config` object both arms print (same keys and values)."""
+    p = scene.params
+    return {"workload": scene.name, "particles": scene.n,
+            "solver_iterations": int(p.num_solver_iterations),
+            "lattice": scene.meta.get("lattice"), "box": scene.meta.get("box"),
+            "grid": [int(g) for g in p.grid], "dt": float(p.timestep),
+            "epsilon": float(p.epsilon), "substeps_timed": K,
+            "window": f"substeps 1-{K} of {scene.substeps}",
+            "l2": "working set > L2 (no flush)",
+            "parallelism": "replicas" if world > 1 else "single"}
+
+
+def reference_arm(args, world: int):
+    """The reference path's CPU implementation (the oracle port) on the host:
+    W warm-up substeps, then the same window as the GPU arm (substeps 1..K
+    from the initial scene), every substep in full.  Only the oracle is
+    loaded: the scene comes from its own generator (oracle/scenes.py)."""
     import oracle
+    from oracle import scenes as oscenes
+    scene = getattr(oscenes, args.scene)()
     threads = oracle.max_threads()
     o = oracle.Oracle(scene.params, scene.n)
     o.set_state(scene.x4, scene.v4)
-    total_steps = args.steps + args.warmup
-    # slice so that the whole run takes about two minutes
-    probe_tot, probe_full, probe_slice = o.sample_substep(0, max(1, scene.n // 256))
-    per_particle = probe_slice / max(1, scene.n // 256)
-    budget = max(0.05, 120.0 / total_steps - probe_full)
-    width = int(min(scene.n, max(1024, budget / max(per_particle, 1e-12))))
-    nslices = max(1, scene.n // width)
-    est = []
-    t0 = time.perf_counter()
-    for k in range(total_steps):
-        lo = (k % nslices) * width
-        tot, _, _ = o.sample_substep(lo, min(scene.n, lo + width))
-        if k >= args.warmup:
-            est.append(tot)
-    wall = time.perf_counter() - t0
+    warm = o.step(max(1, args.warmup))
+    per = warm / max(1, args.warmup)
+    o.set_state(scene.x4, scene.v4)
+    K = args.steps
     it = scene.params.num_solver_iterations
-    sec_per_step = sum(est) / len(est)
+    if per * K <= 240.0:
+        secs = o.step(K)
+        timed = K
+        sample = (f"substeps 1-{K} of the {scene.n}-particle dam break, every substep in "
+                  f"full ({secs:.1f} s wall, FP32 oracle, OpenMP)")
+    else:
+        # bounded: as many whole substeps of the window as fit in ~4 minutes
+        timed = max(1, int(240.0 / per))
+        secs = o.step(timed)
+        sample = (f"substeps 1-{timed} of the {K}-substep window in full ({secs:.1f} s wall, "
+                  f"FP32 oracle, OpenMP)")
+    sec_per_step = secs / timed
     value = scene.n * it / sec_per_step
     return {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
         "warmup": args.warmup, "ms_per_step": sec_per_step * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "impl": "reference",
-        "config": {"workload": scene.name, "particles": scene.n, "solver_iterations": it,
-                   "lattice": scene.meta.get("lattice"), "box": scene.meta.get("box"),
-                   "sample_particles_per_step": width},
+        "config": workload_config(scene, K, world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"each step: predict+sort+cells of all {scene.n} particles, "
-                                   f"solver+commit+vorticity of a {width}-particle sorted slice, "
-                                   f"extrapolated; {wall:.0f} s wall"},
+                         "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "reference = FP32 C++ restatement of pbf's GLSL shaders (the GL path needs an "
-                "OpenGL 4.3 context: unavailable on this box)",
+                "OpenGL 4.3 context: unavailable on this box); only the oracle library is loaded",
     }
+
+
+def _sig(x, digits: int = 4):
+    if isinstance(x, float):
+        return float(f"{x:.{digits}g}")
+    if isinstance(x, list):
+        return [_sig(v, digits) for v in x]
+    if isinstance(x, dict):
+        return {k: _sig(v, digits) for k, v in x.items()}
+    return x
+
+
+def legs_summary(stable, full, batched, adjoint, adjoint5, small, recov) -> dict:
+    """The headline figure of each leg (rounded to 4 digits)."""
+    out = {}
+    if full:
+        out["full_500"] = _sig({"value": full["value"], "ms_per_step": full["ms_per_step"],
+                                "ms_per_step_by_100": full["ms_per_step_by_100"]})
+    if stable:
+        out["stable_500_eps5"] = _sig({"value": stable["value"], "ms_per_step": stable["ms_per_step"]})
+    if small:
+        out["dam_break_16k_200"] = _sig({"value": small["value"], "ms_per_step": small["ms_per_step"],
+                                         "cpu_oracle": (small.get("cpu_oracle") or {}).get("value")})
+    if batched:
+        out["batched_256"] = _sig({"speedup_vs_plain": batched["speedup"],
+                                   "batched_scenes_per_s": batched["batched_scenes_per_s"],
+                                   "bit_identical": batched["bit_identical_sampled_scenes"]})
+    for key, a in (("adjoint_32k", adjoint), ("adjoint_32k_eps5", adjoint5)):
+        if a:
+            out[key] = _sig({"bwd_fwd": a["bwd_fwd_ratio"], "fwd_ms": a["forward_ms"],
+                             "grad_finite": a["grad_finite"]})
+    if recov:
+        for key, r in recov.items():
+            out["recovery_64_eps" + key.split("_")[-1]] = _sig({
+                "ms_per_gd_step": r["ms_per_gd_step"], "loss": [r["loss_first"], r["loss_last"]],
+                "c_err": [r["param_error_start"]["xsph_c"], r["param_error_end"]["xsph_c"]],
+                "vort_err": [r["param_error_start"]["vorticity_epsilon"],
+                             r["param_error_end"]["vorticity_epsilon"]],
+                "nonfinite": r["scene_gradients_nonfinite"]})
+    return out
 
 
 def main():
     args = parse()
     rank, world, local = dist_env()
-    from pbf_gb300 import scenes
-    scene = getattr(scenes, args.scene)()
-
     if args.impl == "reference":
         if rank == 0:
-            print(json.dumps(reference_arm(args, scene)), flush=True)
+            print(json.dumps(reference_arm(args, world)), flush=True)
         return 0
+    from pbf_gb300 import scenes
+    scene = getattr(scenes, args.scene)()
     if world > 1:
         # replicas: the window and e2e lines scale; the single-GPU legs
         # (full runs, batch, adjoint, splatting, the 16k configuration) would
         # only repeat on every rank
         args.no_stable = args.no_full = args.no_batched = args.no_adjoint = True
-        args.no_splat = args.no_small = True
+        args.no_splat = args.no_small = args.no_recovery = True
 
     import torch
     import torch.distributed as dist
@@ -683,7 +741,7 @@ def main():
         splats = splat_leg(stream)
 
     recov = None
-    if args.recovery:
+    if not args.no_recovery:
         recov = {"workload_epsilon_0.01": recovery(stream),
                  "reference_default_epsilon_5": recovery(stream, epsilon=5.0)}
 
@@ -695,7 +753,7 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(scene, args.cpu_substeps)
+        cpu = cpu_baseline(args.scene, args.cpu_substeps)
     small = None
     if not args.no_small:
         small = small_config(stream, rank == 0 and world == 1 and not args.no_cpu_baseline)
@@ -705,13 +763,8 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
             "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": scene.name, "particles": scene.n, "solver_iterations": it,
-                       "lattice": scene.meta.get("lattice"), "box": scene.meta.get("box"),
-                       "grid": list(scene.params.grid), "dt": scene.params.timestep,
-                       "substeps_timed": K, "window": f"substeps 1-{K} of {scene.substeps}",
-                       "l2": "working set > L2 (no flush)",
-                       "parallelism": "replicas" if world > 1 else "single",
-                       "tuning": tuning},
+            "config": workload_config(scene, K, world),
+            "tuning": tuning,
             "e2e": {"value": e2e_value, "unit": UNIT,
                     "h2d_bytes_per_step": 2 * 16 * scene.n, "d2h_bytes_per_step": 2 * 16 * scene.n,
                     "ms_per_step": e2e_ms / E, "steps": E},
@@ -726,17 +779,15 @@ def main():
             "kernel_ms_per_substep": {k: v / counted for k, v in stages.items()},
             "kernel_share": {k: v / total_stage for k, v in stages.items()},
             "gpu_launches": launches,
-            "stable_500": stable,
-            "full_500": full,
-            "batched_256": batched,
-            "adjoint_32k": adjoint,
-            "adjoint_32k_epsilon_5": adjoint5,
-            "splat_reference_scene": splats,
-            "dam_break_16k_200": small,
-            "state_after_window": state_after,
-            "recovery_64": recov,
+            "detail": {"stable_500": stable, "full_500": full, "batched_256": batched,
+                       "adjoint_32k": adjoint, "adjoint_32k_epsilon_5": adjoint5,
+                       "splat_reference_scene": splats, "dam_break_16k_200": small,
+                       "recovery_64": recov, "state_after_window": state_after},
             "clocks": clk,
             "cpu_baseline": cpu,
+            # compact figures of every leg, last on the line so that a
+            # truncated tail of the output still shows them
+            "legs": legs_summary(stable, full, batched, adjoint, adjoint5, small, recov),
         }
         print(json.dumps(line), flush=True)
     if world > 1:

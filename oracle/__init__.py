@@ -25,7 +25,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libpbf_oracle.so")
 SRC = [os.path.join(HERE, "pbf_oracle.cpp"), os.path.join(HERE, "pbf_oracle.hpp"),
-       os.path.join(HERE, "pbf_splat_oracle.cpp")]
+       os.path.join(HERE, "pbf_splat_oracle.cpp"), os.path.join(HERE, "pbf_scene_oracle.cpp"),
+       os.path.join(HERE, "pbf_dual.cpp"), os.path.join(HERE, "pbf_dual.hpp")]
 
 CXXFLAGS = ["-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"]
 
@@ -37,10 +38,17 @@ def build(force: bool = False) -> str:
             os.path.getmtime(LIB) >= os.path.getmtime(s) for s in SRC):
         return LIB
     tmp = LIB + ".tmp"
-    cmd = [os.environ.get("CXX", "g++")] + CXXFLAGS + ["-o", tmp, SRC[0], SRC[2]]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("oracle build failed:\n" + " ".join(cmd) + "\n" + r.stderr)
+    cxx = os.environ.get("CXX", "g++")
+    # the dual-number twin at -O3 (its tangent loops vectorise, ~4x faster);
+    # no flag here changes a floating-point result (no fast-math, no contraction)
+    dual_obj = os.path.join(BUILD, "pbf_dual.o")
+    cmds = [[cxx] + [f for f in CXXFLAGS if f not in ("-O2", "-shared")] +
+            ["-O3", "-c", "-o", dual_obj, SRC[4]],
+            [cxx] + CXXFLAGS + ["-o", tmp, SRC[0], SRC[2], SRC[3], dual_obj]]
+    for cmd in cmds:
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("oracle build failed:\n" + " ".join(cmd) + "\n" + r.stderr)
     os.replace(tmp, LIB)
     return LIB
 
@@ -75,6 +83,18 @@ def load() -> C.CDLL:
         lib.pbfo_max_threads.restype = C.c_int
         lib.pbfo_sample_substep.restype = C.c_double
         lib.pbfo_sample_substep.argtypes = [P, C.c_uint32, C.c_uint32, P, P]
+        lib.pbfo_wpoly6.restype = C.c_double
+        lib.pbfo_wpoly6.argtypes = [C.c_double, C.c_double]
+        lib.pbfo_rest_density_lattice.restype = C.c_double
+        lib.pbfo_rest_density_lattice.argtypes = [C.c_double, C.c_double]
+        lib.pbfo_params_default.restype = C.c_int
+        lib.pbfo_params_default.argtypes = [P, P]
+        lib.pbfo_dual_tangents.restype = C.c_int
+        lib.pbfo_dual_tangents.argtypes = [P, C.c_uint32, P, P, C.c_uint32, C.c_uint32, P, P, P,
+                                           P, P, P, P, C.c_int]
+        lib.pbfo_scene_block.restype = C.c_int
+        lib.pbfo_scene_block.argtypes = [P, C.c_float, P, C.c_float, C.c_float, C.c_float,
+                                         C.c_uint64, P, P]
         _lib = lib
     return _lib
 
@@ -175,6 +195,36 @@ class Oracle:
         self._lib.pbfo_diagnostics(self._h, out.ctypes.data)
         return {"mean_density_error": out[0], "max_density_error": out[1],
                 "kinetic_energy": out[2], "candidate_pairs": out[3]}
+
+
+DUAL_KINDS = {"v": 0, "x": 1, "epsilon": 2, "tensile_instability_k": 3, "xsph_viscosity_c": 4,
+              "vorticity_epsilon": 5}
+
+
+def dual_tangents(params, x4, v4, substeps: int, directions, threads: int = 0):
+    """Forward-mode derivatives of the FP64 twin (pbf_dual.cpp): `directions`
+    is a list of ("v" | "x", index, component) or (scalar name,) tuples.
+    Returns (x_N, v_N, xdot, vdot): the final state (n, 3) in double, equal to
+    the FP64 twin's, and its tangents (ndir, n, 3)."""
+    lib = load()
+    x = np.ascontiguousarray(x4, np.float32)
+    v = np.ascontiguousarray(v4, np.float32)
+    n = x.shape[0]
+    nd = len(directions)
+    kind = np.array([DUAL_KINDS[d[0]] for d in directions], np.int32)
+    idx = np.array([int(d[1]) if len(d) > 1 else 0 for d in directions], np.int32)
+    comp = np.array([int(d[2]) if len(d) > 2 else 0 for d in directions], np.int32)
+    xo = np.empty((n, 3), np.float64)
+    vo = np.empty((n, 3), np.float64)
+    xd = np.empty((nd, n, 3), np.float64)
+    vd = np.empty((nd, n, 3), np.float64)
+    rc = lib.pbfo_dual_tangents(C.addressof(params), n, x.ctypes.data, v.ctypes.data, int(substeps),
+                                nd, kind.ctypes.data, idx.ctypes.data, comp.ctypes.data,
+                                xo.ctypes.data, vo.ctypes.data, xd.ctypes.data, vd.ctypes.data,
+                                int(threads))
+    if rc != 0:
+        raise ValueError("pbfo_dual_tangents: bad argument")
+    return xo, vo, xd, vd
 
 
 def radix_sort(keys, numbits: int):

@@ -52,6 +52,11 @@
 
 namespace pbfo {
 
+// Unqualified fma / sqrt below resolve to these for float and double, and by
+// argument-dependent lookup to the dual-number overloads of pbf_dual.hpp.
+using std::fma;
+using std::sqrt;
+
 // Same layout as pbf_params in include/pbf.h (checked by the tests).
 struct Params {
     float one_over_rho_0;
@@ -91,18 +96,18 @@ static inline V3<T> scale3(V3<T> a, T s) {
 // dot(a, b) = fma(az, bz, fma(ay, by, ax * bx))
 template <typename T>
 static inline T dot3(V3<T> a, V3<T> b) {
-    return std::fma(a.z, b.z, std::fma(a.y, b.y, a.x * b.x));
+    return fma(a.z, b.z, fma(a.y, b.y, a.x * b.x));
 }
 // cross(a, b) with one fused multiply-add per component
 template <typename T>
 static inline V3<T> cross3(V3<T> a, V3<T> b) {
-    return {std::fma(a.y, b.z, -(a.z * b.y)), std::fma(a.z, b.x, -(a.x * b.z)),
-            std::fma(a.x, b.y, -(a.y * b.x))};
+    return {fma(a.y, b.z, -(a.z * b.y)), fma(a.z, b.x, -(a.x * b.z)),
+            fma(a.x, b.y, -(a.y * b.x))};
 }
 // acc + s * a, fused per component
 template <typename T>
 static inline V3<T> fma3(T s, V3<T> a, V3<T> acc) {
-    return {std::fma(s, a.x, acc.x), std::fma(s, a.y, acc.y), std::fma(s, a.z, acc.z)};
+    return {fma(s, a.x, acc.x), fma(s, a.y, acc.y), fma(s, a.z, acc.z)};
 }
 
 // Poly6 normalisation 315/(64 pi) and spiky normalisation 15/pi as the
@@ -162,10 +167,14 @@ static inline uint32_t cell_coord(T x, T G, uint32_t Gi) {
     return ic < Gi ? ic : Gi - 1;
 }
 
+// min(max(q, lo), hi) (updatepos.glsl:100)
+static inline float clamp_wall(float q, float lo, float hi) { return std::min(std::max(q, lo), hi); }
+static inline double clamp_wall(double q, double lo, double hi) { return std::min(std::max(q, lo), hi); }
+
 // Wpoly6 for len <= h: k6 * ((h^2 - len^2)^3)  with t = fma(-len, len, h^2).
 template <typename T>
 static inline T w_poly6(const Consts<T>& c, T len) {
-    T t = std::fma(-len, len, c.h2);
+    T t = fma(-len, len, c.h2);
     return ((t * t) * t) * c.k6;
 }
 
@@ -400,7 +409,7 @@ struct Sim {
             V3<T> gi{0, 0, 0};
             for_each_neighbour(i, [&](uint32_t j) {
                 const V3<T> d = sub3(pi, P[j]);
-                const T len = std::sqrt(dot3(d, d));
+                const T len = sqrt(dot3(d, d));
                 if (len > c.h) return;           // Wpoly6 and gradWspiky are 0
                 rho = rho + w_poly6(c, len);     // :80-82
                 if (len == (T)0) return;         // gradWspiky(0) = 0 (:60)
@@ -409,7 +418,7 @@ struct Sim {
                 gi = add3(gi, g);                // :93
             });
             sumk = sumk + dot3(gi, gi);                  // :97
-            const T Ci = std::fma(rho, c.oorho, (T)-1);  // :100
+            const T Ci = fma(rho, c.oorho, (T)-1);  // :100
             lambda[i] = -Ci / (sumk + c.eps);            // :101
         }
     }
@@ -427,7 +436,7 @@ struct Sim {
             V3<T> dp{0, 0, 0};
             for_each_neighbour(i, [&](uint32_t j) {
                 const V3<T> d = sub3(pi, P[j]);
-                const T len = std::sqrt(dot3(d, d));
+                const T len = sqrt(dot3(d, d));
                 if (len > c.h || len == (T)0) return;  // gradWspiky = 0
                 T sc = c.scale * w_poly6(c, len);      // :57
                 sc = sc * sc;                          // :58
@@ -439,9 +448,9 @@ struct Sim {
             });
             V3<T> q = fma3(c.oorho, dp, pi);  // :85
             // clamp (:100)
-            q.x = std::min(std::max(q.x, c.lo[0]), c.hi[0]);
-            q.y = std::min(std::max(q.y, c.lo[1]), c.hi[1]);
-            q.z = std::min(std::max(q.z, c.lo[2]), c.hi[2]);
+            q.x = clamp_wall(q.x, c.lo[0], c.hi[0]);
+            q.y = clamp_wall(q.y, c.lo[1], c.hi[1]);
+            q.z = clamp_wall(q.z, c.lo[2], c.hi[2]);
             Q[i] = q;
         }
     }
@@ -474,7 +483,7 @@ struct Sim {
             for_each_neighbour(i, [&](uint32_t j) {
                 const V3<T> vij = sub3(vs[j], vi);  // :50
                 const V3<T> d = sub3(pi, P[j]);     // :51
-                const T len = std::sqrt(dot3(d, d));
+                const T len = sqrt(dot3(d, d));
                 if (len > c.h) return;
                 const T wp = w_poly6(c, len);  // :52
                 acc = fma3(wp, vij, acc);      // :54
@@ -484,7 +493,7 @@ struct Sim {
             });
             vx[i] = fma3(c.cx, acc, vi);         // :58
             om[i] = w;
-            omag[i] = std::sqrt(dot3(w, w));     // :60
+            omag[i] = sqrt(dot3(w, w));     // :60
         }
 #pragma omp parallel for schedule(dynamic, 256) num_threads(nt)
         for (int64_t ii = lo; ii < hi; ++ii) {
@@ -493,12 +502,12 @@ struct Sim {
             V3<T> eta{0, 0, 0};
             for_each_neighbour(i, [&](uint32_t j) {
                 const V3<T> d = sub3(pi, P[j]);  // :69
-                const T len = std::sqrt(dot3(d, d));
+                const T len = sqrt(dot3(d, d));
                 if (len > c.h || len == (T)0) return;
                 const V3<T> g = scale3(d, grad_scale(c.kg, c.h, len));
                 eta = fma3(omag[j], g, eta);  // :72
             });
-            const T l = std::sqrt(dot3(eta, eta));  // :76
+            const T l = sqrt(dot3(eta, eta));  // :76
             if (l > (T)0) eta = {eta.x / l, eta.y / l, eta.z / l};  // :77-78
             v[perm[i]] = fma3(c.dteps, cross3(eta, om[i]), vx[i]);  // :82,85
         }
@@ -593,7 +602,7 @@ struct Sim {
             T rho = 0;
             for_each_neighbour(i, [&](uint32_t j) {
                 const V3<T> d = sub3(pi, xpred[j]);
-                const T len = std::sqrt(dot3(d, d));
+                const T len = sqrt(dot3(d, d));
                 if (len > c.h) return;
                 rho = rho + w_poly6(c, len);
             });

@@ -226,3 +226,38 @@ def test_zero_iterations_and_no_vorticity(oracle_mod):
     xs = sc.x4[:, 1] + dt * vy
     assert np.array_equal(x[:, 1], xs.astype(np.float32))
     assert np.array_equal(v[:, 1], ((xs - sc.x4[:, 1]) / dt).astype(np.float32))
+
+
+def test_oracle_scenes_equal_the_product_generator(oracle_mod, product_lib):
+    """bench.py's CPU reference arm builds its scenes with the oracle's own
+    generator (so it never loads the product library); the scenes and the
+    folded constants must be the same bytes as the product's."""
+    from oracle import scenes as oscenes
+    assert C.sizeof(oscenes.Params) == C.sizeof(Params)
+    assert [f for f, _ in oscenes.Params._fields_] == [f for f, _ in Params._fields_]
+    for name in ("plain_16k", "plain_2m"):
+        a, b = getattr(oscenes, name)(), getattr(scenes, name)()
+        assert a.name == b.name and a.substeps == b.substeps and a.meta == b.meta
+        assert bytes(a.params) == bytes(b.params), name
+        assert np.array_equal(a.x4.view(np.uint32), b.x4.view(np.uint32)), name
+        assert np.array_equal(a.v4.view(np.uint32), b.v4.view(np.uint32)), name
+    (oa, ob), (pa, pb) = oscenes.diff_32k(), scenes.diff_32k()
+    for u, w in ((oa, pa), (ob, pb)):
+        assert bytes(u.params) == bytes(w.params)
+        assert np.array_equal(u.x4.view(np.uint32), w.x4.view(np.uint32))
+        assert np.array_equal(u.v4.view(np.uint32), w.v4.view(np.uint32))
+    # uniform and normal velocity draws, other origins and spacings
+    for kw in ({"vel_uniform": 0.5, "seed": 3}, {"vel_sigma": 0.25, "seed": 9, "spacing": 0.37},
+               {"vel_uniform": 0.2, "vel_sigma": 0.1, "origin": (1.5, 0.25, 7.0), "seed": 2**63 + 5}):
+        xa, va = oscenes.block((5, 7, 3), **kw)
+        xb, vb = scenes.block((5, 7, 3), **kw)
+        assert np.array_equal(xa.view(np.uint32), xb.view(np.uint32))
+        assert np.array_equal(va.view(np.uint32), vb.view(np.uint32))
+    for h, s in ((1.0, 0.5), (2.0, 0.94), (0.7, 0.33)):
+        assert oscenes.rest_density(h, s) == scenes.rest_density(h, s)
+        assert oscenes.wpoly6(0.3 * h, h) == scenes.wpoly6(0.3 * h, h)
+    for grid in ((128, 64, 128), (20, 8, 40)):
+        po, pp = oscenes.Params(), Params()
+        assert oracle_mod.load().pbfo_params_default((C.c_uint32 * 3)(*grid), C.addressof(po)) == 0
+        assert product_lib.pbf_params_default((C.c_uint32 * 3)(*grid), C.byref(pp)) == 0
+        assert bytes(po) == bytes(pp)
