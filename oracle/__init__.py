@@ -89,9 +89,10 @@ def load() -> C.CDLL:
         lib.pbfo_rest_density_lattice.argtypes = [C.c_double, C.c_double]
         lib.pbfo_params_default.restype = C.c_int
         lib.pbfo_params_default.argtypes = [P, P]
-        lib.pbfo_dual_tangents.restype = C.c_int
-        lib.pbfo_dual_tangents.argtypes = [P, C.c_uint32, P, P, C.c_uint32, C.c_uint32, P, P, P,
-                                           P, P, P, P, C.c_int]
+        for fn in (lib.pbfo_dual_tangents, lib.pbfo_dual_tangents_fp32):
+            fn.restype = C.c_int
+            fn.argtypes = [P, C.c_uint32, P, P, C.c_uint32, C.c_uint32, P, P, P, P, P, P, P,
+                           C.c_int]
         lib.pbfo_scene_block.restype = C.c_int
         lib.pbfo_scene_block.argtypes = [P, C.c_float, P, C.c_float, C.c_float, C.c_float,
                                          C.c_uint64, P, P]
@@ -201,11 +202,12 @@ DUAL_KINDS = {"v": 0, "x": 1, "epsilon": 2, "tensile_instability_k": 3, "xsph_vi
               "vorticity_epsilon": 5}
 
 
-def dual_tangents(params, x4, v4, substeps: int, directions, threads: int = 0):
-    """Forward-mode derivatives of the FP64 twin (pbf_dual.cpp): `directions`
-    is a list of ("v" | "x", index, component) or (scalar name,) tuples.
-    Returns (x_N, v_N, xdot, vdot): the final state (n, 3) in double, equal to
-    the FP64 twin's, and its tangents (ndir, n, 3)."""
+def dual_tangents(params, x4, v4, substeps: int, directions, threads: int = 0, fp32: bool = False):
+    """Forward-mode derivatives of the FP64 twin (pbf_dual.cpp), or with
+    fp32=True of the FP32 oracle's own trajectory: `directions` is a list of
+    ("v" | "x", index, component) or (scalar name,) tuples.  Returns
+    (x_N, v_N, xdot, vdot): the final state (n, 3) in double, equal to the
+    FP64 twin's (or the FP32 oracle's), and its tangents (ndir, n, 3)."""
     lib = load()
     x = np.ascontiguousarray(x4, np.float32)
     v = np.ascontiguousarray(v4, np.float32)
@@ -218,7 +220,8 @@ def dual_tangents(params, x4, v4, substeps: int, directions, threads: int = 0):
     vo = np.empty((n, 3), np.float64)
     xd = np.empty((nd, n, 3), np.float64)
     vd = np.empty((nd, n, 3), np.float64)
-    rc = lib.pbfo_dual_tangents(C.addressof(params), n, x.ctypes.data, v.ctypes.data, int(substeps),
+    fn = lib.pbfo_dual_tangents_fp32 if fp32 else lib.pbfo_dual_tangents
+    rc = fn(C.addressof(params), n, x.ctypes.data, v.ctypes.data, int(substeps),
                                 nd, kind.ctypes.data, idx.ctypes.data, comp.ctypes.data,
                                 xo.ctypes.data, vo.ctypes.data, xd.ctypes.data, vd.ctypes.data,
                                 int(threads))
@@ -283,17 +286,23 @@ def ref_load() -> C.CDLL:
         lib.pbfr_substep_highlight.restype = C.c_int
         lib.pbfr_splat.argtypes = [C.c_int, P, C.c_uint32, P, P, C.c_uint32, C.c_uint32, P]
         lib.pbfr_splat.restype = C.c_int
+        lib.pbfr_set_cell_fix.argtypes = [C.c_int]
+        lib.pbfr_set_cell_fix.restype = None
         _ref = lib
     return _ref
 
 
-def ref_substep(params, x4, v4, highlight=None):
+def ref_substep(params, x4, v4, highlight=None, cell_fix: int = 2):
     """One SPH::Run of the reference's shaders.  Returns a dict with x, v (id
     order), sorted ids, the grid start/end textures (x fastest, then y, z),
     the packed neighbour texture (n, 3, 4) and lambda (sorted order); with
     `highlight` (uint32[n] flags, id order) also the flags after the
-    clearhighlight / highlight dispatches of that substep."""
+    clearhighlight / highlight dispatches of that substep.  `cell_fix`
+    (ref_driver.cpp's pbfr_set_cell_fix): by default the end of the last
+    occupied cell, which findcells never writes, is n, so that its run stays
+    inside the particle buffer."""
     lib = ref_load()
+    lib.pbfr_set_cell_fix(int(cell_fix))
     n = x4.shape[0]
     x = np.ascontiguousarray(x4, np.float32).copy()
     v = np.ascontiguousarray(v4, np.float32).copy()

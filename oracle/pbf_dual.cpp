@@ -8,23 +8,13 @@
 namespace {
 
 constexpr int kLanes = 16;
-using D = pbfo::Dual<kLanes>;
 
-}  // namespace
-
-extern "C" {
-
-// Tangents of the final state of `substeps` substeps along `ndir` directions.
-// Direction k seeds kind[k]: 0 = v0[idx[k]][comp[k]], 1 = x0[idx[k]][comp[k]],
-// 2 = epsilon, 3 = s_corr k (tensile_instability_k), 4 = XSPH c,
-// 5 = vorticity epsilon.  Outputs (any may be NULL): x_out, v_out[n * 3]
-// (the final state's value, equal to the FP64 twin's), xdot, vdot[ndir * n * 3]
-// (d final state / d direction).  Runs ceil(ndir / 16) passes of the dual
-// simulation.  Returns 0, or 1 on a bad argument.
-int pbfo_dual_tangents(const pbfo::Params* prm, uint32_t n, const float* x4, const float* v4,
-                       uint32_t substeps, uint32_t ndir, const int32_t* kind, const int32_t* idx,
-                       const int32_t* comp, double* x_out, double* v_out, double* xdot,
-                       double* vdot, int nthreads) {
+template <typename V>
+int dual_tangents(const pbfo::Params* prm, uint32_t n, const float* x4, const float* v4,
+                  uint32_t substeps, uint32_t ndir, const int32_t* kind, const int32_t* idx,
+                  const int32_t* comp, double* x_out, double* v_out, double* xdot, double* vdot,
+                  int nthreads) {
+    using D = pbfo::DualT<V, kLanes>;
     if (!prm || !x4 || !v4 || (ndir && (!kind || !idx || !comp))) return 1;
     for (uint32_t k = 0; k < ndir; ++k) {
         if (kind[k] < 0 || kind[k] > 5) return 1;
@@ -50,21 +40,21 @@ int pbfo_dual_tangents(const pbfo::Params* prm, uint32_t n, const float* x4, con
                 case 2: s.c.eps.d[lane] = 1.0; break;
                 case 3: s.c.negk.d[lane] = -1.0; break;  // negk = -k
                 case 4: s.c.cx.d[lane] = 1.0; break;
-                case 5: s.c.dteps.d[lane] = (double)prm->timestep; break;  // dteps = dt * eps_v
+                case 5: s.c.dteps.d[lane] = (double)(V)prm->timestep; break;  // dteps = dt * eps_v
             }
         }
         for (uint32_t t = 0; t < substeps; ++t) s.substep();
         if (pass == 0) {
             for (uint32_t i = 0; i < n; ++i) {
                 if (x_out) {
-                    x_out[3 * i] = s.x[i].x.v;
-                    x_out[3 * i + 1] = s.x[i].y.v;
-                    x_out[3 * i + 2] = s.x[i].z.v;
+                    x_out[3 * i] = (double)s.x[i].x.v;
+                    x_out[3 * i + 1] = (double)s.x[i].y.v;
+                    x_out[3 * i + 2] = (double)s.x[i].z.v;
                 }
                 if (v_out) {
-                    v_out[3 * i] = s.v[i].x.v;
-                    v_out[3 * i + 1] = s.v[i].y.v;
-                    v_out[3 * i + 2] = s.v[i].z.v;
+                    v_out[3 * i] = (double)s.v[i].x.v;
+                    v_out[3 * i + 1] = (double)s.v[i].y.v;
+                    v_out[3 * i + 2] = (double)s.v[i].z.v;
                 }
             }
         }
@@ -86,6 +76,36 @@ int pbfo_dual_tangents(const pbfo::Params* prm, uint32_t n, const float* x4, con
         }
     }
     return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Tangents of the final state of `substeps` substeps along `ndir` directions.
+// Direction k seeds kind[k]: 0 = v0[idx[k]][comp[k]], 1 = x0[idx[k]][comp[k]],
+// 2 = epsilon, 3 = s_corr k (tensile_instability_k), 4 = XSPH c,
+// 5 = vorticity epsilon.  Outputs (any may be NULL): x_out, v_out[n * 3]
+// (the final state's value, equal to the FP64 twin's), xdot, vdot[ndir * n * 3]
+// (d final state / d direction).  Runs ceil(ndir / 16) passes of the dual
+// simulation.  Returns 0, or 1 on a bad argument.
+int pbfo_dual_tangents(const pbfo::Params* prm, uint32_t n, const float* x4, const float* v4,
+                       uint32_t substeps, uint32_t ndir, const int32_t* kind, const int32_t* idx,
+                       const int32_t* comp, double* x_out, double* v_out, double* xdot,
+                       double* vdot, int nthreads) {
+    return dual_tangents<double>(prm, n, x4, v4, substeps, ndir, kind, idx, comp, x_out, v_out,
+                                 xdot, vdot, nthreads);
+}
+
+// The same on the FP32 oracle's trajectory: the value part equals the FP32
+// oracle (and so the GPU) bit for bit; the tangents are the derivatives of
+// that FP32 program, carried in double.
+int pbfo_dual_tangents_fp32(const pbfo::Params* prm, uint32_t n, const float* x4, const float* v4,
+                            uint32_t substeps, uint32_t ndir, const int32_t* kind,
+                            const int32_t* idx, const int32_t* comp, double* x_out,
+                            double* v_out, double* xdot, double* vdot, int nthreads) {
+    return dual_tangents<float>(prm, n, x4, v4, substeps, ndir, kind, idx, comp, x_out, v_out,
+                                xdot, vdot, nthreads);
 }
 
 }  // extern "C"

@@ -21,8 +21,9 @@
 // Decisions on the reference's undefined or buggy behaviour:
 //   Q1  h is a parameter; the stencil is the 27 cells around the particle's
 //       cell as in the reference, so h <= 1 makes it complete.
-//   Q2  cell coordinate = min(int(clamp(x, 0, G)), G - 1) per axis, used for
-//       the key AND the stencil centre, so every position has a valid cell.
+//   Q2  key cell coordinate = min(int(clamp(x, 0, G)), G - 1) per axis, so
+//       every position has a valid cell; the stencil centre is the reference's
+//       unclamped int(x) (neighbourcells.glsl:57), see stencil_coord.
 //   Q3  start[cell(x_0)] = 0 and end[cell(x_{N-1})] = N; empty cells -1.
 //   Q4  stencil cells outside the grid are empty.
 //   Q5  Jacobi everywhere: each stage reads only the previous stage's output.
@@ -165,6 +166,20 @@ static inline uint32_t cell_coord(T x, T G, uint32_t Gi) {
     c = (c <= G) ? c : G;
     uint32_t ic = (uint32_t)c;
     return ic < Gi ? ic : Gi - 1;
+}
+
+// Stencil centre along one axis: ivec3(particlekeys[i].xyz) of
+// neighbourcells.glsl:57, the predicted coordinate truncated toward zero with
+// no clamp, so a particle predicted outside the grid looks for neighbours
+// around that outside cell (rows and cells outside the grid are empty,
+// decision Q4).  Saturated to [-2, G + 1], which leaves the runs unchanged
+// (every row of a centre beyond that lies outside the grid); NaN maps to 0.
+template <typename T>
+static inline int stencil_coord(T x, uint32_t Gi) {
+    if (!(x == x)) return 0;
+    if (x <= (T)-2) return -2;
+    if (x >= (T)Gi + (T)1) return (int)Gi + 1;
+    return (int)x;
 }
 
 // min(max(q, lo), hi) (updatepos.glsl:100)
@@ -356,11 +371,9 @@ struct Sim {
     // empty runs have begin == end).
     void runs_of(uint32_t i, int32_t rb[9], int32_t re[9]) const {
         const uint32_t Gx = p.grid[0], Gy = p.grid[1], Gz = p.grid[2];
-        const uint32_t k = sorted_keys[i];
-        const int cx = (int)(k % Gx);
-        const uint32_t rem = k / Gx;
-        const int cz = (int)(rem % Gz);
-        const int cy = (int)(rem / Gz);
+        const int cx = stencil_coord<T>(xpred[i].x, Gx);
+        const int cy = stencil_coord<T>(xpred[i].y, Gy);
+        const int cz = stencil_coord<T>(xpred[i].z, Gz);
         int o = 0;
         for (int dy = -1; dy <= 1; ++dy)
             for (int dz = -1; dz <= 1; ++dz, ++o) {

@@ -63,11 +63,23 @@ struct Rec {
 };
 static_assert(sizeof(Rec) == 16, "particle key record");
 
+// Switches (off by default) for findcells.glsl:39-43's two boundary cells,
+// the oracle's decision Q3: bit 0 gives the first sorted particle's cell its
+// start (0), bit 1 the last one's cell its end (n).  The reference never
+// writes that end; on a GPU the texture then holds whatever it held, here a
+// fresh 0, so the last cell's packed count goes negative and its run reads
+// past the particle buffer in some scenes (GL robust access would hide that).
+// Bit 1 keeps such a scene's run in bounds; bit 0 separates the first-cell
+// quirk from the rest of the reference's behaviour in multi-step comparisons.
+int g_cell_fix = 0;
+
 }  // namespace
 
 extern "C" {
 
 int pbfr_record_size(void) { return (int)sizeof(Rec); }
+
+void pbfr_set_cell_fix(int on) { g_cell_fix = on; }
 
 // One substep.  x4, v4 (float4, id order) are updated in place.  Optional
 // outputs: sorted ids [n], grid start/end textures [Gx*Gy*Gz] (x fastest,
@@ -127,6 +139,18 @@ int pbfr_substep_highlight(const Params* p, uint32_t n, float* x4, float* v4, ui
     for (uint32_t g = 0; g < n; ++g) {
         set_invocation(g);
         sh_findcells::main_invocation();
+    }
+    if (g_cell_fix && n > 0) {
+        auto texel = [&](const Rec& r) {
+            const ivec3 c = ivec3(clamp(vec3(r.x, r.y, r.z), vec3(0.0f, 0.0f, 0.0f), G::GRID_SIZE));
+            return (size_t)c.x + (size_t)gx * ((size_t)c.y + (size_t)gy * (size_t)c.z);
+        };
+        const size_t first = texel(sorted[0]), last = texel(sorted[n - 1]);
+        if (g_cell_fix & 1) {
+            if (first != 0) start[0] = -1;  // undo thread 0's fixed store
+            if (first < cells) start[first] = 0;
+        }
+        if ((g_cell_fix & 2) && last < cells) end[last] = (int32_t)n;
     }
     sh_neighbourcells::particlekeys = reinterpret_cast<vec4*>(sorted.data());
     sh_neighbourcells::gridtexture = isampler3D{start.data(), gx, gy, gz};

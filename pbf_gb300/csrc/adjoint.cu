@@ -50,7 +50,7 @@ struct Tape {
     std::vector<float4*> ckpt_x, ckpt_v;  // states at substeps 0, every, 2 every, ... (id order)
     float4 *final_x = nullptr, *final_v = nullptr;
     struct Slot {
-        uint32_t *perm = nullptr, *skeys = nullptr;
+        uint32_t* perm = nullptr;
         int32_t *cstart = nullptr, *cend = nullptr;
         std::vector<float4*> L, AUX;
         float4 *PF = nullptr, *VS = nullptr, *OM = nullptr, *Q = nullptr, *ETA = nullptr;
@@ -158,18 +158,18 @@ __device__ __forceinline__ void adj_replay(uint32_t i, const AdjLists& al, F&& f
     }
 }
 
-template <class F>
-__device__ __forceinline__ void adj_scan_eval(uint32_t i, uint32_t key, const DevConsts& c,
+template <class Ctr, class F>
+__device__ __forceinline__ void adj_scan_eval(uint32_t i, Ctr&& ctr, const DevConsts& c,
                                               const int32_t* __restrict__ cstart,
                                               const int32_t* __restrict__ cend,
                                               const float4* __restrict__ X, float3 pi,
                                               const AdjLists& al, F&& f) {
     if (!al.cap) {
-        visit_full(i, key, c, cstart, cend, f);
+        visit_full(i, ctr, c, cstart, cend, f);
         return;
     }
     Runs r;
-    runs_of(key, c, cstart, cend, r);
+    runs_of(ctr(), c, cstart, cend, r);
     uint32_t tot = 0;
     uint32_t* const out = al.idx + i;
 #pragma unroll 1
@@ -202,19 +202,19 @@ __device__ __forceinline__ void adj_scan_eval(uint32_t i, uint32_t key, const De
         adj_replay(i, al, f);
     } else {
         al.cnt[i] = -1;
-        visit_full(i, key, c, cstart, cend, f);
+        visit_full(i, ctr, c, cstart, cend, f);
     }
 }
 
-template <class F>
-__device__ __forceinline__ void adj_visit_again(uint32_t i, uint32_t key, const DevConsts& c,
+template <class Ctr, class F>
+__device__ __forceinline__ void adj_visit_again(uint32_t i, Ctr&& ctr, const DevConsts& c,
                                                 const int32_t* __restrict__ cstart,
                                                 const int32_t* __restrict__ cend,
                                                 const AdjLists& al, F&& f) {
     if (al.cap && al.cnt[i] >= 0)
         adj_replay(i, al, f);
     else
-        visit_full(i, key, c, cstart, cend, f);
+        visit_full(i, ctr, c, cstart, cend, f);
 }
 
 // Constants of particle `id` (scene lookup by id for batches).
@@ -259,7 +259,7 @@ k_adj_vort_b1(const uint32_t* __restrict__ perm, const float4* __restrict__ VB,
 // and the position adjoint, then folds |w|-bar into w-bar.
 template <class CP>
 __global__ void __launch_bounds__(kAdjBlock)
-k_adj_vort_b2(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ skeys,
+k_adj_vort_b2(const uint32_t* __restrict__ perm, const float4* __restrict__ XPc,
               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
               const float4* __restrict__ Q, const float4* __restrict__ OM,
               const float4* __restrict__ ETB, float4* __restrict__ OMB, float4* __restrict__ PA,
@@ -274,7 +274,7 @@ k_adj_vort_b2(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ sk
     const float3 ebi = f3(ETB[i]);
     float mb = 0.0f;
     float3 pb = make_float3(0.0f, 0.0f, 0.0f);
-    adj_scan_eval(i, skeys[i], c, cstart, cend, Q, pi, al, [&](uint32_t j) {
+    adj_scan_eval(i, [&] { return stencil_centre(XPc[i], c); }, c, cstart, cend, Q, pi, al, [&](uint32_t j) {
         const float4 Qj = __ldg(Q + j);
         const float3 d = pi - f3(Qj);
         const float r2 = dotf(d, d);
@@ -294,7 +294,7 @@ k_adj_vort_b2(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ sk
 // committed-velocity adjoint and adds the position adjoint; accumulates d/dc.
 template <class CP>
 __global__ void __launch_bounds__(kAdjBlock)
-k_adj_vort_a(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ skeys,
+k_adj_vort_a(const uint32_t* __restrict__ perm, const float4* __restrict__ XPc,
              const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
              const float4* __restrict__ PF, const float4* __restrict__ VS,
              const float4* __restrict__ VSB, const float4* __restrict__ OMB,
@@ -311,7 +311,7 @@ k_adj_vort_a(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ ske
     float3 vb = sbi;
     float3 pb = f3(PA[i]);
     float3 wsum = make_float3(0.0f, 0.0f, 0.0f);
-    adj_visit_again(i, skeys[i], c, cstart, cend, al, [&](uint32_t j) {
+    adj_visit_again(i, [&] { return stencil_centre(XPc[i], c); }, c, cstart, cend, al, [&](uint32_t j) {
         const float3 d = pi - f3(__ldg(PF + j));
         const float r2 = dotf(d, d);
         if (r2 > c.r2cut) return;
@@ -364,7 +364,7 @@ k_adj_commit(const uint32_t* __restrict__ perm, const float4* __restrict__ XB,
 // accumulates d/d(eps) and d/dk.
 template <class CP>
 __global__ void __launch_bounds__(kAdjBlock)
-k_adj_delta_p(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ skeys,
+k_adj_delta_p(const uint32_t* __restrict__ perm, const float4* __restrict__ XPc,
               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
               const float4* __restrict__ L, const float4* __restrict__ AUX,
               const float4* __restrict__ QB, float4* __restrict__ PDB, float4* __restrict__ RS,
@@ -381,7 +381,7 @@ k_adj_delta_p(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ sk
     float lb = 0.0f, kb = 0.0f;
     float3 pb = qbi;
     const float sc4 = c.scale * c.scale * c.scale * c.scale;
-    adj_scan_eval(i, skeys[i], c, cstart, cend, L, pi, al, [&](uint32_t j) {
+    adj_scan_eval(i, [&] { return stencil_centre(XPc[i], c); }, c, cstart, cend, L, pi, al, [&](uint32_t j) {
         const float4 Lj = __ldg(L + j);
         const float3 d = pi - f3(Lj);
         const float r2 = dotf(d, d);
@@ -416,7 +416,7 @@ k_adj_delta_p(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ sk
 // the predicted-position adjoint after the first iteration.
 template <class CP>
 __global__ void __launch_bounds__(kAdjBlock)
-k_adj_lambda(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ skeys,
+k_adj_lambda(const uint32_t* __restrict__ perm, const float4* __restrict__ XPc,
              const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
              const float4* __restrict__ L, const float4* __restrict__ AUX,
              const float4* __restrict__ RS, const float4* __restrict__ PDB,
@@ -430,7 +430,7 @@ k_adj_lambda(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ ske
     const float4 RSi = RS[i];
     const float3 gi = f3(AUX[i]);
     float3 pb = f3(PDB[i]);
-    adj_visit_again(i, skeys[i], c, cstart, cend, al, [&](uint32_t j) {
+    adj_visit_again(i, [&] { return stencil_centre(XPc[i], c); }, c, cstart, cend, al, [&](uint32_t j) {
         const float3 d = pi - f3(__ldg(L + j));
         const float r2 = dotf(d, d);
         if (r2 > c.r2cut) return;
@@ -490,7 +490,6 @@ cudaError_t alloc_tape(pbf_sim* s, Tape* t) {
     t->slots.resize(t->nslots);
     for (auto& sl : t->slots) {
         if (e == cudaSuccess) e = talloc(t, &sl.perm, n);
-        if (e == cudaSuccess) e = talloc(t, &sl.skeys, n);
         if (e == cudaSuccess) e = talloc(t, &sl.cstart, s->ncells);
         if (e == cudaSuccess) e = talloc(t, &sl.cend, s->ncells);
         sl.L.assign(t->iters, nullptr);
@@ -528,18 +527,18 @@ cudaError_t reverse_substep(pbf_sim* s, Tape* t, const Tape::Slot& sl, const CP&
     if (t->vort) {
         k_adj_vort_b1<<<g, kAdjBlock, 0, st>>>(sl.perm, t->VB, sl.OM, sl.ETA, t->VSB, t->ETB,
                                                t->OMB, acc_ev, n, cp);
-        k_adj_vort_b2<<<g, kAdjBlock, 0, st>>>(sl.perm, sl.skeys, sl.cstart, sl.cend, sl.Q, sl.OM,
+        k_adj_vort_b2<<<g, kAdjBlock, 0, st>>>(sl.perm, sl.PF, sl.cstart, sl.cend, sl.Q, sl.OM,
                                                t->ETB, t->OMB, t->PA, al, n, cp);
-        k_adj_vort_a<<<g, kAdjBlock, 0, st>>>(sl.perm, sl.skeys, sl.cstart, sl.cend, sl.PF, sl.VS,
+        k_adj_vort_a<<<g, kAdjBlock, 0, st>>>(sl.perm, sl.PF, sl.cstart, sl.cend, sl.PF, sl.VS,
                                               t->VSB, t->OMB, t->VCB, t->PA, acc_c, al, n, cp);
     }
     k_adj_commit<<<g, kAdjBlock, 0, st>>>(sl.perm, t->XB, t->VB, t->VCB, t->PA, sl.PF, t->QB,
                                           t->XOB, t->XSB, t->vort ? 1 : 0, iters, n, cp);
     for (int k = iters - 1; k >= 0; --k) {
-        k_adj_delta_p<<<g, kAdjBlock, 0, st>>>(sl.perm, sl.skeys, sl.cstart, sl.cend, sl.L[k],
+        k_adj_delta_p<<<g, kAdjBlock, 0, st>>>(sl.perm, sl.PF, sl.cstart, sl.cend, sl.L[k],
                                                sl.AUX[k], t->QB, t->PDB, t->RS, acc_eps, acc_k, al,
                                                n, cp);
-        k_adj_lambda<<<g, kAdjBlock, 0, st>>>(sl.perm, sl.skeys, sl.cstart, sl.cend, sl.L[k],
+        k_adj_lambda<<<g, kAdjBlock, 0, st>>>(sl.perm, sl.PF, sl.cstart, sl.cend, sl.L[k],
                                               sl.AUX[k], t->RS, t->PDB, t->QB, t->XSB,
                                               k == 0 ? 1 : 0, al, n, cp);
     }
@@ -573,8 +572,6 @@ cudaError_t record_segment(pbf_sim* s, Tape* t, uint32_t count) {
         e = enqueue_substep(s, nullptr, &rec);
         if (e != cudaSuccess) return e;
         e = cudaMemcpyAsync(sl.perm, s->perm, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(sl.skeys, s->skeys, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(sl.cstart, s->cstart, sizeof(int32_t) * s->ncells,
                                 cudaMemcpyDeviceToDevice, st);

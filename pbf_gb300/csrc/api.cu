@@ -490,7 +490,7 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
     if (mixed) {
         cudaError_t me = cudaMemsetAsync(s->heavy_count, 0, sizeof(uint32_t), st);
         if (me != cudaSuccess) return me;
-        launch_heavy_scan(g, st, s->skeys, s->cstart, s->cend, s->tuning.coop_candidates, n, cps,
+        launch_heavy_scan(g, st, s->XP, s->cstart, s->cend, s->tuning.coop_candidates, n, cps,
                           s->heavy, s->heavy_list, s->heavy_count);
     }
     mark(3);
@@ -1218,9 +1218,9 @@ pbf_status pbf_highlight_neighbours(pbf_sim* s, uint32_t* flags, int where) {
     const unsigned g = grid_for(s->n);
     // the sorted particle's scene for batches comes from the sorted scene ids
     if (s->nscenes == 1)
-        launch_highlight(g, st, s->skeys, s->perm, s->cstart, s->cend, d, s->n, OneScene{s->dc});
+        launch_highlight(g, st, s->XP, s->perm, s->cstart, s->cend, d, s->n, OneScene{s->dc});
     else
-        launch_highlight(g, st, s->skeys, s->perm, s->cstart, s->cend, d, s->n,
+        launch_highlight(g, st, s->XP, s->perm, s->cstart, s->cend, d, s->n,
                          ManyScenes{s->d_consts, s->sid_sorted});
     PBF_CUDA(s, cudaGetLastError());
     if (where == PBF_HOST) {

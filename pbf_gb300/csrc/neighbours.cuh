@@ -6,20 +6,36 @@
 
 namespace pbf {
 
-// Sorted-index ranges of the 9 stencil rows of a cell (neighbourcells.glsl:52-90).
+// Sorted-index ranges of the 9 stencil rows around a centre (neighbourcells.glsl:52-90).
 struct Runs {
     int32_t b[9], e[9];
 };
 
-__device__ __forceinline__ void runs_of(uint32_t key, const DevConsts& c,
+// Stencil centre along one axis (neighbourcells.glsl:57): the predicted
+// coordinate truncated toward zero, NOT clamped.  A particle predicted outside
+// the grid (below the floor, say) searches around that outside cell, and the
+// rows and cells outside the grid are empty (decision Q4), so it finds fewer
+// neighbours or none, as in the reference.  Saturated to [-2, G + 1], which
+// leaves the runs unchanged; NaN maps to 0.
+__device__ __forceinline__ int stencil_coord(float x, uint32_t Gi) {
+    if (!(x == x)) return 0;
+    if (x <= -2.0f) return -2;
+    if (x >= fadd(__uint2float_rn(Gi), 1.0f)) return (int)Gi + 1;
+    return __float2int_rz(x);
+}
+__device__ __forceinline__ int3 stencil_centre(float3 q, const DevConsts& c) {
+    return make_int3(stencil_coord(q.x, c.Gi[0]), stencil_coord(q.y, c.Gi[1]),
+                     stencil_coord(q.z, c.Gi[2]));
+}
+__device__ __forceinline__ int3 stencil_centre(float4 q, const DevConsts& c) {
+    return stencil_centre(make_float3(q.x, q.y, q.z), c);
+}
+
+__device__ __forceinline__ void runs_of(int3 ctr, const DevConsts& c,
                                         const int32_t* __restrict__ cstart,
                                         const int32_t* __restrict__ cend, Runs& r) {
     const uint32_t Gx = c.Gi[0], Gy = c.Gi[1], Gz = c.Gi[2];
-    const uint32_t local = key - c.cell_base;
-    const int cx = (int)(local % Gx);
-    const uint32_t rem = local / Gx;
-    const int cz = (int)(rem % Gz);
-    const int cy = (int)(rem / Gz);
+    const int cx = ctr.x, cy = ctr.y, cz = ctr.z;
     const int xlo = cx > 0 ? cx - 1 : 0;
     const int xhi = cx + 1 < (int)Gx ? cx + 1 : (int)Gx - 1;
 #pragma unroll
@@ -42,14 +58,17 @@ __device__ __forceinline__ void runs_of(uint32_t key, const DevConsts& c,
 }
 
 
-template <class F>
-__device__ __forceinline__ void visit_full(uint32_t i, uint32_t key, const DevConsts& c,
+// `ctr` returns the stencil centre (stencil_centre of the sweep's predicted
+// position): the visits call it where they build the runs, so no centre stays
+// live in registers across the neighbour loops.
+template <class Ctr, class F>
+__device__ __forceinline__ void visit_full(uint32_t i, Ctr&& ctr, const DevConsts& c,
                                            const int32_t* __restrict__ cstart,
                                            const int32_t* __restrict__ cend, F&& f) {
     // The 9 ranges live in a small local array: computing each row inside the
     // loop instead raises register use and lowers occupancy (measured slower).
     Runs r;
-    runs_of(key, c, cstart, cend, r);
+    runs_of(ctr(), c, cstart, cend, r);
 #pragma unroll 1
     for (int o = 0; o < 9; ++o)
         for (int32_t j = r.b[o]; j < r.e[o]; ++j)
@@ -93,19 +112,16 @@ constexpr uint32_t kRunMin = 4;
 //  - otherwise f runs on each.
 // The visit then resumes at r.  Every other candidate goes to f.  pos(j) is
 // the position the sweep tests at (the set `runs` was built from).
-template <class Pos, class F, class G, class U>
-__device__ __forceinline__ void visit_direct_piles(uint32_t i, uint32_t key, const DevConsts& c,
+template <class Ctr, class Pos, class F, class G, class U>
+__device__ __forceinline__ void visit_direct_piles(uint32_t i, Ctr&& ctr, const DevConsts& c,
                                                    const int32_t* __restrict__ cstart,
                                                    const int32_t* __restrict__ cend,
                                                    const uint32_t* __restrict__ runs, Pos&& pos,
                                                    float3 pi, F&& f, G&& coincident,
                                                    U&& uniform) {
     const uint32_t Gx = c.Gi[0], Gy = c.Gi[1], Gz = c.Gi[2];
-    const uint32_t local = key - c.cell_base;
-    const int cx = (int)(local % Gx);
-    const uint32_t rem = local / Gx;
-    const int cz = (int)(rem % Gz);
-    const int cy = (int)(rem / Gz);
+    const int3 cc = ctr();
+    const int cx = cc.x, cy = cc.y, cz = cc.z;
     const int xlo = cx > 0 ? cx - 1 : 0;
     const int xhi = cx + 1 < (int)Gx ? cx + 1 : (int)Gx - 1;
 #pragma unroll 1
@@ -182,13 +198,13 @@ __device__ __forceinline__ uint32_t spread_even(uint32_t x) {
 // the run (an odd run start or end) and i itself are masked out once per
 // chunk.  With LIST, `list(base, mask)` also receives, per chunk, the
 // candidates base + t (bit t) with r2 <= c.r2list, before f runs on the chunk.
-template <bool LIST, class S, class F>
-__device__ __forceinline__ void visit_masked(uint32_t i, uint32_t key, const DevConsts& c,
+template <bool LIST, class Ctr, class S, class F>
+__device__ __forceinline__ void visit_masked(uint32_t i, Ctr&& ctr, const DevConsts& c,
                                              const int32_t* __restrict__ cstart,
                                              const int32_t* __restrict__ cend, const ScanPos& X,
                                              float3 pi, S&& list, F&& f) {
     Runs r;
-    runs_of(key, c, cstart, cend, r);
+    runs_of(ctr(), c, cstart, cend, r);
     const float2 px = make_float2(pi.x, pi.x), py = make_float2(pi.y, pi.y),
                  pz = make_float2(pi.z, pi.z), neg = make_float2(-1.0f, -1.0f);
     const float cut = c.r2cut;

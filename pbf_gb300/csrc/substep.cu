@@ -220,15 +220,15 @@ __device__ __forceinline__ void warp_max_to(uint32_t* slot, float v) {
 }
 
 // The full-stencil visit of a sweep: direct, or scan-then-evaluate by chunks.
-template <bool MASKED, class F>
-__device__ __forceinline__ void sweep_visit(uint32_t i, uint32_t key, const DevConsts& c,
+template <bool MASKED, class Ctr, class F>
+__device__ __forceinline__ void sweep_visit(uint32_t i, Ctr&& ctr, const DevConsts& c,
                                             const int32_t* __restrict__ cstart,
                                             const int32_t* __restrict__ cend, const ScanPos& X,
                                             float3 pi, F&& body) {
     if constexpr (MASKED)
-        visit_masked<false>(i, key, c, cstart, cend, X, pi, [](int32_t, uint32_t) {}, body);
+        visit_masked<false>(i, ctr, c, cstart, cend, X, pi, [](int32_t, uint32_t) {}, body);
     else
-        visit_full(i, key, c, cstart, cend, body);
+        visit_full(i, ctr, c, cstart, cend, body);
 }
 
 // Masked stencil scan with the pair list recorded first and the pair bodies
@@ -239,8 +239,8 @@ __device__ __forceinline__ void sweep_visit(uint32_t i, uint32_t key, const DevC
 // sweeps) instead of chunk by chunk.  A list longer than its capacity keeps
 // its first `cap` entries (and is marked -1 for the replaying sweep); the
 // candidates past them are found by a second scan and evaluated in order.
-template <bool LIST, class S, class F>
-__device__ __forceinline__ void scan_then_eval(uint32_t i, uint32_t key, const DevConsts& c,
+template <bool LIST, class Ctr, class S, class F>
+__device__ __forceinline__ void scan_then_eval(uint32_t i, Ctr&& ctr, const DevConsts& c,
                                                const int32_t* __restrict__ cstart,
                                                const int32_t* __restrict__ cend,
                                                const ScanPos& X, float3 pi, const PairLists& pw,
@@ -248,7 +248,7 @@ __device__ __forceinline__ void scan_then_eval(uint32_t i, uint32_t key, const D
     uint32_t* const out = pw.idx + i;
     const size_t stride = pw.n;
     uint32_t tot = 0;
-    visit_masked<LIST>(i, key, c, cstart, cend, X, pi, list, [&](uint32_t j) {
+    visit_masked<LIST>(i, ctr, c, cstart, cend, X, pi, list, [&](uint32_t j) {
         if (tot < pw.cap) out[(size_t)tot * stride] = j;
         ++tot;
     });
@@ -265,7 +265,7 @@ __device__ __forceinline__ void scan_then_eval(uint32_t i, uint32_t key, const D
     }
     if (tot > pw.cap) {
         uint32_t rank = 0;
-        visit_masked<false>(i, key, c, cstart, cend, X, pi, [](int32_t, uint32_t) {},
+        visit_masked<false>(i, ctr, c, cstart, cend, X, pi, [](int32_t, uint32_t) {},
                             [&](uint32_t j) {
                                 if (rank++ >= pw.cap) eval(j);
                             });
@@ -354,6 +354,7 @@ k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys
     if (live) {
         const auto& c = cp.at(i);
         pi = xyz(XP[i]);
+        auto ctr = [&] { return stencil_centre(pi, c); };  // neighbourcells.glsl:57
         LambdaAcc a{0.0f, 0.0f, make_float3(0.0f, 0.0f, 0.0f)};
         int32_t cnt = 0;
         const uint32_t cap = (LISTS && c.use_lists) ? nl.cap : 0u;
@@ -371,15 +372,15 @@ k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys
         };
         if constexpr (MODE == kPairs) {
             if (LISTS && cap)
-                scan_then_eval<true>(i, skeys[i], c, cstart, cend, sx, pi, pw, list_rec, eval);
+                scan_then_eval<true>(i, ctr, c, cstart, cend, sx, pi, pw, list_rec, eval);
             else
-                scan_then_eval<false>(i, skeys[i], c, cstart, cend, sx, pi, pw,
+                scan_then_eval<false>(i, ctr, c, cstart, cend, sx, pi, pw,
                                       [](int32_t, uint32_t) {}, eval);
         } else if constexpr (MODE == kMasked) {
             if (LISTS && cap)
-                visit_masked<true>(i, skeys[i], c, cstart, cend, sx, pi, list_rec, eval);
+                visit_masked<true>(i, ctr, c, cstart, cend, sx, pi, list_rec, eval);
             else
-                visit_masked<false>(i, skeys[i], c, cstart, cend, sx, pi,
+                visit_masked<false>(i, ctr, c, cstart, cend, sx, pi,
                                     [](int32_t, uint32_t) {}, eval);
         } else {
             bool piles = false;
@@ -387,7 +388,7 @@ k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys
                 if (pw.runs) {
                     // a coincident neighbour adds W(0) to the density (:80-82)
                     visit_direct_piles(
-                        i, skeys[i], c, cstart, cend, pw.runs,
+                        i, ctr, c, cstart, cend, pw.runs,
                         [&](uint32_t j) { return xyz(__ldg(XP + j)); }, pi,
                         [&](uint32_t j) {
                             const float3 d = sub3(pi, xyz(__ldg(XP + j)));
@@ -403,7 +404,7 @@ k_lambda_build(const float4* __restrict__ XP, const uint32_t* __restrict__ skeys
                 }
             }
             if (!piles)
-                visit_full(i, skeys[i], c, cstart, cend, [&](uint32_t j) {
+                visit_full(i, ctr, c, cstart, cend, [&](uint32_t j) {
                     const float3 d = sub3(pi, xyz(__ldg(XP + j)));
                     const float r2 = dot3(d, d);
                     if (LISTS && r2 <= c.r2list) {
@@ -436,6 +437,7 @@ k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
     if (i >= n || (pw.heavy && pw.heavy[i])) return;
     const auto& c = cp.at(i);
     const float3 pi = xyz(P[i]);
+    auto ctr = [&] { return stencil_centre(XP[i], c); };  // neighbourcells.glsl:57
     LambdaAcc a{0.0f, 0.0f, make_float3(0.0f, 0.0f, 0.0f)};
     auto eval = [&](uint32_t j) {
         const float3 d = sub3(pi, xyz(__ldg(P + j)));
@@ -463,18 +465,18 @@ k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
     }
     if (!listed) {
         if constexpr (MODE == kPairs)
-            scan_then_eval<false>(i, skeys[i], c, cstart, cend, sx, pi, pw, [](int32_t, uint32_t) {},
+            scan_then_eval<false>(i, ctr, c, cstart, cend, sx, pi, pw, [](int32_t, uint32_t) {},
                                   eval);
         else if (MODE == kDirect && !LISTS && pw.runs)
             visit_direct_piles(
-                i, skeys[i], c, cstart, cend, pw.runs,
+                i, ctr, c, cstart, cend, pw.runs,
                 [&](uint32_t j) { return xyz(__ldg(P + j)); }, pi, eval,
                 [&](uint32_t, uint32_t, uint32_t m) { a.rho = repeat_add(a.rho, w_poly6(c, 0.0f), m); },
                 [&](uint32_t j0, uint32_t r, float3 d, float r2) {
                     lambda_pair_run(c, d, r2, r - j0, a);
                 });
         else
-            sweep_visit<MODE == kMasked>(i, skeys[i], c, cstart, cend, sx, pi, eval);
+            sweep_visit<MODE == kMasked>(i, ctr, c, cstart, cend, sx, pi, eval);
     }
     L[i] = make_float4(pi.x, pi.y, pi.z, lambda_finish(c, a));
     if (aux) aux[i] = lambda_aux(a);
@@ -514,6 +516,7 @@ k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
             dp = fma3(coef, g, dp);                      // :65
         };
         const float3 xi = xyz(XP[i]);
+        auto ctr = [&] { return stencil_centre(XP[i], c); };  // neighbourcells.glsl:57
         bool done = false;
         if constexpr (MODE == kPairs) done = visit_pairs(i, pr, body);
         if (!done) {
@@ -528,7 +531,7 @@ k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
             if (!listed) {
                 if (MODE == kDirect && !LISTS && pr.runs)  // coincident: no term (:56)
                     visit_direct_piles(
-                        i, skeys[i], c, cstart, cend, pr.runs,
+                        i, ctr, c, cstart, cend, pr.runs,
                         [&](uint32_t j) { return xyz(__ldg(L + j)); }, pi, body, [](uint32_t, uint32_t, uint32_t) {},
                         [&](uint32_t j0, uint32_t r, float3 d, float r2) {
                             // the same offset for the run: only lambda_j differs
@@ -543,7 +546,7 @@ k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
                                 dp = fma3(fadd(fadd(li, __ldg(&L[j].w)), sc), g, dp);  // :65
                         });
                 else
-                    sweep_visit<MODE != kDirect>(i, skeys[i], c, cstart, cend, sx, pi, body);
+                    sweep_visit<MODE != kDirect>(i, ctr, c, cstart, cend, sx, pi, body);
             }
         }
         float3 q = fma3(c.oorho, dp, pi);  // :85
@@ -587,15 +590,15 @@ __device__ __forceinline__ float3 shf3(float3 v, int src) {
 // Calls term(j, d, r2) on every in-range candidate's own lane (returning
 // whether the candidate has a term), then fold(src_lane) on all lanes for
 // each in-range candidate with a term, in visit order.
-template <class T, class Fo>
-__device__ __forceinline__ void coop_visit(uint32_t i, uint32_t key, const DevConsts& c,
+template <class Ctr, class T, class Fo>
+__device__ __forceinline__ void coop_visit(uint32_t i, Ctr&& ctr, const DevConsts& c,
                                            const int32_t* __restrict__ cstart,
                                            const int32_t* __restrict__ cend,
                                            const float4* __restrict__ X, float3 pi, T&& term,
                                            Fo&& fold) {
     const uint32_t lane = threadIdx.x & 31u;
     Runs r;
-    runs_of(key, c, cstart, cend, r);
+    runs_of(ctr(), c, cstart, cend, r);
 #pragma unroll 1
     for (int o = 0; o < 9; ++o) {
         const int32_t e = r.e[o];
@@ -635,17 +638,18 @@ struct CoopWork {
 
 template <class CP>
 __global__ void __launch_bounds__(kBlock)
-k_lambda_coop(const float4* __restrict__ P, const uint32_t* __restrict__ skeys,
+k_lambda_coop(const float4* __restrict__ P, const float4* __restrict__ XP,
               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
               float4* __restrict__ L, float4* __restrict__ aux, uint32_t n, CP cp, CoopWork wk) {
     PBF_COOP_FOR_EACH(i) {
         const auto& c = cp.at(i);
         const float3 pi = xyz(P[i]);
+        auto ctr = [&] { return stencil_centre(XP[i], c); };  // neighbourcells.glsl:57
         LambdaAcc a{0.0f, 0.0f, make_float3(0.0f, 0.0f, 0.0f)};
         float tw = 0.0f, tgg = 0.0f;
         float3 tg = make_float3(0.0f, 0.0f, 0.0f);
         bool tgrad = false;
-        coop_visit(i, skeys[i], c, cstart, cend, P, pi,
+        coop_visit(i, ctr, c, cstart, cend, P, pi,
                    [&](uint32_t, float3 d, float r2) {
                        const float len = fsqrt(r2);
                        tw = w_poly6(c, len);
@@ -675,7 +679,7 @@ k_lambda_coop(const float4* __restrict__ P, const uint32_t* __restrict__ skeys,
 
 template <class CP>
 __global__ void __launch_bounds__(kBlock)
-k_delta_p_coop(const float4* __restrict__ L, const uint32_t* __restrict__ skeys,
+k_delta_p_coop(const float4* __restrict__ L, const float4* __restrict__ XP,
                const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
                float4* __restrict__ Pn, ScanPos sx_out, uint32_t n, CP cp, uint32_t* status,
                CoopWork wk) {
@@ -684,10 +688,11 @@ k_delta_p_coop(const float4* __restrict__ L, const uint32_t* __restrict__ skeys,
         const float4 Li = L[i];
         const float3 pi = xyz(Li);
         const float li = Li.w;
+        auto ctr = [&] { return stencil_centre(XP[i], c); };  // neighbourcells.glsl:57
         float3 dp = make_float3(0.0f, 0.0f, 0.0f);
         float tcoef = 0.0f;
         float3 tg = make_float3(0.0f, 0.0f, 0.0f);
-        coop_visit(i, skeys[i], c, cstart, cend, L, pi,
+        coop_visit(i, ctr, c, cstart, cend, L, pi,
                    [&](uint32_t j, float3 d, float r2) {
                        const float len = fsqrt(r2);
                        if (len == 0.0f) return false;
@@ -718,7 +723,7 @@ k_delta_p_coop(const float4* __restrict__ L, const uint32_t* __restrict__ skeys,
 template <class CP>
 __global__ void __launch_bounds__(kBlock)
 k_vorticity_a_coop(const float4* __restrict__ P, const float4* __restrict__ VS,
-                   const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cstart,
+                   const float4* __restrict__ XP, const int32_t* __restrict__ cstart,
                    const int32_t* __restrict__ cend, float4* __restrict__ VX,
                    float4* __restrict__ OM, float4* __restrict__ Q, uint32_t n, CP cp,
                    CoopWork wk) {
@@ -726,11 +731,12 @@ k_vorticity_a_coop(const float4* __restrict__ P, const float4* __restrict__ VS,
         const auto& c = cp.at(i);
         const float3 pi = xyz(P[i]);
         const float3 vi = xyz(VS[i]);
+        auto ctr = [&] { return stencil_centre(XP[i], c); };  // neighbourcells.glsl:57
         float3 acc = make_float3(0.0f, 0.0f, 0.0f), w = make_float3(0.0f, 0.0f, 0.0f);
         float tw = 0.0f;
         float3 tv = make_float3(0.0f, 0.0f, 0.0f), tc = make_float3(0.0f, 0.0f, 0.0f);
         bool tgrad = false;
-        coop_visit(i, skeys[i], c, cstart, cend, P, pi,
+        coop_visit(i, ctr, c, cstart, cend, P, pi,
                    [&](uint32_t j, float3 d, float r2) {
                        const float len = fsqrt(r2);
                        tv = sub3(xyz(__ldg(VS + j)), vi);  // vorticity.glsl:50
@@ -757,17 +763,18 @@ k_vorticity_a_coop(const float4* __restrict__ P, const float4* __restrict__ VS,
 template <class CP>
 __global__ void __launch_bounds__(kBlock)
 k_vorticity_b_coop(const float4* __restrict__ Q, const float4* __restrict__ VX,
-                   const float4* __restrict__ OM, const uint32_t* __restrict__ skeys,
+                   const float4* __restrict__ OM, const float4* __restrict__ XP,
                    const uint32_t* __restrict__ perm, const int32_t* __restrict__ cstart,
                    const int32_t* __restrict__ cend, float4* __restrict__ v,
                    float4* __restrict__ eta_out, uint32_t n, CP cp, CoopWork wk) {
     PBF_COOP_FOR_EACH(i) {
         const auto& c = cp.at(i);
         const float3 pi = xyz(Q[i]);
+        auto ctr = [&] { return stencil_centre(XP[i], c); };  // neighbourcells.glsl:57
         float3 eta = make_float3(0.0f, 0.0f, 0.0f);
         float tq = 0.0f;
         float3 tg = make_float3(0.0f, 0.0f, 0.0f);
-        coop_visit(i, skeys[i], c, cstart, cend, Q, pi,
+        coop_visit(i, ctr, c, cstart, cend, Q, pi,
                    [&](uint32_t j, float3 d, float r2) {
                        const float len = fsqrt(r2);
                        if (len == 0.0f) return false;
@@ -794,7 +801,7 @@ k_vorticity_b_coop(const float4* __restrict__ Q, const float4* __restrict__ VX,
 // consecutive warps of a cooperative launch work on neighbouring particles.
 template <class CP>
 __global__ void __launch_bounds__(kBlock)
-k_heavy_scan(const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cstart,
+k_heavy_scan(const float4* __restrict__ XP, const int32_t* __restrict__ cstart,
              const int32_t* __restrict__ cend, uint32_t threshold, uint32_t n, CP cp,
              uint8_t* __restrict__ heavy, uint32_t* __restrict__ list, uint32_t* __restrict__ count) {
     __shared__ uint32_t warp_off[kBlock / 32];
@@ -804,7 +811,7 @@ k_heavy_scan(const uint32_t* __restrict__ skeys, const int32_t* __restrict__ cst
     bool h = false;
     if (i < n) {
         Runs r;
-        runs_of(skeys[i], cp.at(i), cstart, cend, r);
+        runs_of(stencil_centre(XP[i], cp.at(i)), cp.at(i), cstart, cend, r);
         uint32_t cand = 0;
 #pragma unroll
         for (int o = 0; o < 9; ++o) cand += (uint32_t)(r.e[o] - r.b[o]);
@@ -868,6 +875,7 @@ k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
     const auto& c = cp.at(i);
     const float3 pi = xyz(P[i]);
     const float3 vi = xyz(VS[i]);
+    auto ctr = [&] { return stencil_centre(XP[i], c); };  // neighbourcells.glsl:57
     float3 acc = make_float3(0.0f, 0.0f, 0.0f), w = make_float3(0.0f, 0.0f, 0.0f);
     auto eval = [&](uint32_t j) {
         const float3 d = sub3(pi, xyz(__ldg(P + j)));  // :51
@@ -900,11 +908,11 @@ k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
     }
     if (!listed) {
         if constexpr (MODE == kPairs)
-            scan_then_eval<false>(i, skeys[i], c, cstart, cend, sx, pi, pw, [](int32_t, uint32_t) {},
+            scan_then_eval<false>(i, ctr, c, cstart, cend, sx, pi, pw, [](int32_t, uint32_t) {},
                                   eval);
         else if (MODE == kDirect && !LISTS && pw.runs)
             visit_direct_piles(
-                i, skeys[i], c, cstart, cend, pw.runs,
+                i, ctr, c, cstart, cend, pw.runs,
                 [&](uint32_t j) { return xyz(__ldg(P + j)); }, pi, eval,
                 [&](uint32_t j0, uint32_t r, uint32_t) {  // len 0: W(0) (v_j - v_i), no curl
                     const float w0 = w_poly6(c, 0.0f);
@@ -923,7 +931,7 @@ k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
                     }
                 });
         else
-            sweep_visit<MODE == kMasked>(i, skeys[i], c, cstart, cend, sx, pi, eval);
+            sweep_visit<MODE == kMasked>(i, ctr, c, cstart, cend, sx, pi, eval);
     }
     const float3 vx = fma3(c.cx, acc, vi);  // :58
     VX[i] = make_float4(vx.x, vx.y, vx.z, 0.0f);
@@ -945,6 +953,7 @@ k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ XP,
     if (i >= n || (pr.heavy && pr.heavy[i])) return;
     const auto& c = cp.at(i);
     const float3 pi = xyz(Q[i]);
+    auto ctr = [&] { return stencil_centre(XP[i], c); };  // neighbourcells.glsl:57
     float3 eta = make_float3(0.0f, 0.0f, 0.0f);
     auto body = [&](uint32_t j) {
         const float4 Qj = __ldg(Q + j);
@@ -969,7 +978,7 @@ k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ XP,
         if (!listed) {
             if (MODE == kDirect && !LISTS && pr.runs)  // coincident: no term (:71)
                 visit_direct_piles(
-                    i, skeys[i], c, cstart, cend, pr.runs,
+                    i, ctr, c, cstart, cend, pr.runs,
                     [&](uint32_t j) { return xyz(__ldg(Q + j)); }, pi, body, [](uint32_t, uint32_t, uint32_t) {},
                     [&](uint32_t j0, uint32_t r, float3 d, float r2) {
                         // the same offset for the run: only |omega_j| differs
@@ -979,7 +988,7 @@ k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ XP,
                             eta = fma3(__ldg(&Q[j].w), g, eta);  // :72
                     });
             else
-                sweep_visit<MODE != kDirect>(i, skeys[i], c, cstart, cend, sx, pi, body);
+                sweep_visit<MODE != kDirect>(i, ctr, c, cstart, cend, sx, pi, body);
         }
     }
     if (eta_out) eta_out[i] = make_float4(eta.x, eta.y, eta.z, 0.0f);
@@ -1000,9 +1009,9 @@ k_diagnostics(const float4* __restrict__ P, const float4* __restrict__ v,
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const auto& c = cp.at(i);
-    Runs r;
-    runs_of(skeys[i], c, cstart, cend, r);
     const float3 pi = xyz(P[i]);
+    Runs r;
+    runs_of(stencil_centre(pi, c), c, cstart, cend, r);
     float rho = 0.0f;
     int32_t cand = -1;
     for (int o = 0; o < 9; ++o) {
@@ -1026,7 +1035,7 @@ k_diagnostics(const float4* __restrict__ P, const float4* __restrict__ v,
 // flags are in id order; the candidates come from the last substep's sort.
 template <class CP>
 __global__ void __launch_bounds__(kBlock)
-k_highlight(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
+k_highlight(const float4* __restrict__ XP, const uint32_t* __restrict__ perm,
             const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
             uint32_t* flags, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1034,7 +1043,7 @@ k_highlight(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ per
     const uint32_t id = perm[i];
     if (id >= n || (flags[id] & 1u) == 0u) return;
     const auto& c = cp.at(i);
-    visit_full(i, skeys[i], c, cstart, cend, [&](uint32_t j) {
+    visit_full(i, [&] { return stencil_centre(XP[i], c); }, c, cstart, cend, [&](uint32_t j) {
         const uint32_t pj = perm[j];
         if (pj < n) atomicOr(flags + pj, 2u);
     });
@@ -1046,16 +1055,16 @@ __global__ void __launch_bounds__(kBlock) k_clear_highlight(uint32_t* flags, uin
 }
 
 template <class CP>
-void launch_highlight(unsigned g, cudaStream_t st, const uint32_t* skeys, const uint32_t* perm,
+void launch_highlight(unsigned g, cudaStream_t st, const float4* XP, const uint32_t* perm,
                       const int32_t* cstart, const int32_t* cend, uint32_t* flags, uint32_t n,
                       CP cp) {
     k_clear_highlight<<<g, kBlock, 0, st>>>(flags, n);
-    k_highlight<CP><<<g, kBlock, 0, st>>>(skeys, perm, cstart, cend, flags, n, cp);
+    k_highlight<CP><<<g, kBlock, 0, st>>>(XP, perm, cstart, cend, flags, n, cp);
 }
-template void launch_highlight<OneScene>(unsigned, cudaStream_t, const uint32_t*, const uint32_t*,
+template void launch_highlight<OneScene>(unsigned, cudaStream_t, const float4*, const uint32_t*,
                                          const int32_t*, const int32_t*, uint32_t*, uint32_t,
                                          OneScene);
-template void launch_highlight<ManyScenes>(unsigned, cudaStream_t, const uint32_t*,
+template void launch_highlight<ManyScenes>(unsigned, cudaStream_t, const float4*,
                                            const uint32_t*, const int32_t*, const int32_t*,
                                            uint32_t*, uint32_t, ManyScenes);
 
@@ -1090,13 +1099,13 @@ void launch_lambda_build(SweepCfg sw, cudaStream_t st, const float4* XP, const u
                          const int32_t* cstart, const int32_t* cend, float4* L, float4* aux,
                          NbrLists nl, PairLists pw, ScanPos sx, uint32_t n, CP cp) {
     if (sw.mode == kCoop) {
-        k_lambda_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(XP, skeys, cstart, cend, L, aux, n, cp,
+        k_lambda_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(XP, XP, cstart, cend, L, aux, n, cp,
                                                            CoopWork{nullptr, nullptr});
         return;
     }
     PBF_SWEEP_LAUNCH(k_lambda_build, XP, skeys, cstart, cend, L, aux, nl, pw, sx, n, cp);
     if (pw.heavy)
-        k_lambda_coop<CP><<<kHeavyGrid, kBlock, 0, st>>>(XP, skeys, cstart, cend, L, aux, n, cp,
+        k_lambda_coop<CP><<<kHeavyGrid, kBlock, 0, st>>>(XP, XP, cstart, cend, L, aux, n, cp,
                                                          CoopWork{pw.heavy_list, pw.heavy_count});
 }
 template <class CP>
@@ -1105,13 +1114,13 @@ void launch_lambda(SweepCfg sw, cudaStream_t st, const float4* P, const float4* 
                    float4* aux, NbrLists nl, PairLists pw, ScanPos sx, int dmax_slot, uint32_t n,
                    CP cp) {
     if (sw.mode == kCoop) {
-        k_lambda_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(P, skeys, cstart, cend, L, aux, n, cp,
+        k_lambda_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(P, XP, cstart, cend, L, aux, n, cp,
                                                            CoopWork{nullptr, nullptr});
         return;
     }
     PBF_SWEEP_LAUNCH(k_lambda, P, XP, skeys, cstart, cend, L, aux, nl, pw, sx, dmax_slot, n, cp);
     if (pw.heavy)
-        k_lambda_coop<CP><<<kHeavyGrid, kBlock, 0, st>>>(P, skeys, cstart, cend, L, aux, n, cp,
+        k_lambda_coop<CP><<<kHeavyGrid, kBlock, 0, st>>>(P, XP, cstart, cend, L, aux, n, cp,
                                                          CoopWork{pw.heavy_list, pw.heavy_count});
 }
 template <class CP>
@@ -1120,7 +1129,7 @@ void launch_delta_p(SweepCfg sw, cudaStream_t st, const float4* L, const float4*
                     NbrLists nl, PairLists pr, ScanPos sx, ScanPos sx_out, int dmax_slot,
                     int out_slot, uint32_t n, CP cp, uint32_t* status) {
     if (sw.mode == kCoop) {
-        k_delta_p_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(L, skeys, cstart, cend, Pn,
+        k_delta_p_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(L, XP, cstart, cend, Pn,
                                                             ScanPos{nullptr, nullptr}, n, cp, status,
                                                             CoopWork{nullptr, nullptr});
         return;
@@ -1128,15 +1137,15 @@ void launch_delta_p(SweepCfg sw, cudaStream_t st, const float4* L, const float4*
     PBF_SWEEP_LAUNCH(k_delta_p, L, XP, skeys, cstart, cend, Pn, nl, pr, sx, sx_out, dmax_slot,
                      out_slot, n, cp, status);
     if (pr.heavy)
-        k_delta_p_coop<CP><<<kHeavyGrid, kBlock, 0, st>>>(L, skeys, cstart, cend, Pn, sx_out, n, cp,
+        k_delta_p_coop<CP><<<kHeavyGrid, kBlock, 0, st>>>(L, XP, cstart, cend, Pn, sx_out, n, cp,
                                                           status,
                                                           CoopWork{pr.heavy_list, pr.heavy_count});
 }
 template <class CP>
-void launch_heavy_scan(unsigned g, cudaStream_t st, const uint32_t* skeys, const int32_t* cstart,
+void launch_heavy_scan(unsigned g, cudaStream_t st, const float4* XP, const int32_t* cstart,
                        const int32_t* cend, uint32_t threshold, uint32_t n, CP cp, uint8_t* heavy,
                        uint32_t* list, uint32_t* count) {
-    k_heavy_scan<CP><<<g, kBlock, 0, st>>>(skeys, cstart, cend, threshold, n, cp, heavy, list, count);
+    k_heavy_scan<CP><<<g, kBlock, 0, st>>>(XP, cstart, cend, threshold, n, cp, heavy, list, count);
 }
 template <class CP>
 void launch_commit(unsigned g, cudaStream_t st, const float4* P, const uint32_t* perm, float4* x,
@@ -1149,7 +1158,7 @@ void launch_vorticity_a(SweepCfg sw, cudaStream_t st, const float4* P, const flo
                         const int32_t* cend, float4* VX, float4* OM, float4* Q, NbrLists nl,
                         PairLists pw, ScanPos sx, int dmax_slot, uint32_t n, CP cp) {
     if (sw.mode == kCoop) {
-        k_vorticity_a_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(P, VS, skeys, cstart, cend, VX, OM, Q,
+        k_vorticity_a_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(P, VS, XP, cstart, cend, VX, OM, Q,
                                                                n, cp, CoopWork{nullptr, nullptr});
         return;
     }
@@ -1157,7 +1166,7 @@ void launch_vorticity_a(SweepCfg sw, cudaStream_t st, const float4* P, const flo
                      n, cp);
     if (pw.heavy)
         k_vorticity_a_coop<CP><<<kHeavyGrid, kBlock, 0, st>>>(
-            P, VS, skeys, cstart, cend, VX, OM, Q, n, cp, CoopWork{pw.heavy_list, pw.heavy_count});
+            P, VS, XP, cstart, cend, VX, OM, Q, n, cp, CoopWork{pw.heavy_list, pw.heavy_count});
 }
 template <class CP>
 void launch_vorticity_b(SweepCfg sw, cudaStream_t st, const float4* Q, const float4* XP,
@@ -1166,7 +1175,7 @@ void launch_vorticity_b(SweepCfg sw, cudaStream_t st, const float4* Q, const flo
                         float4* v, float4* eta_out, NbrLists nl, PairLists pr, ScanPos sx,
                         int dmax_slot, uint32_t n, CP cp) {
     if (sw.mode == kCoop) {
-        k_vorticity_b_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(Q, VX, OM, skeys, perm, cstart, cend, v,
+        k_vorticity_b_coop<CP><<<coop_grid(n), kBlock, 0, st>>>(Q, VX, OM, XP, perm, cstart, cend, v,
                                                                eta_out, n, cp, CoopWork{nullptr, nullptr});
         return;
     }
@@ -1174,7 +1183,7 @@ void launch_vorticity_b(SweepCfg sw, cudaStream_t st, const float4* Q, const flo
                      dmax_slot, n, cp);
     if (pr.heavy)
         k_vorticity_b_coop<CP><<<kHeavyGrid, kBlock, 0, st>>>(
-            Q, VX, OM, skeys, perm, cstart, cend, v, eta_out, n, cp,
+            Q, VX, OM, XP, perm, cstart, cend, v, eta_out, n, cp,
             CoopWork{pr.heavy_list, pr.heavy_count});
 }
 template <class CP>
@@ -1199,7 +1208,7 @@ void launch_diagnostics(unsigned g, cudaStream_t st, const float4* P, const floa
                                      const uint32_t*, const int32_t*, const int32_t*, float4*,  \
                                      NbrLists, PairLists, ScanPos, ScanPos, int, int, uint32_t, \
                                      CP, uint32_t*);                                            \
-    template void launch_heavy_scan<CP>(unsigned, cudaStream_t, const uint32_t*, const int32_t*,  \
+    template void launch_heavy_scan<CP>(unsigned, cudaStream_t, const float4*, const int32_t*,    \
                                         const int32_t*, uint32_t, uint32_t, CP, uint8_t*,          \
                                         uint32_t*, uint32_t*);                                     \
     template void launch_commit<CP>(unsigned, cudaStream_t, const float4*, const uint32_t*,     \

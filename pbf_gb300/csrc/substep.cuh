@@ -54,7 +54,7 @@ void launch_delta_p(SweepCfg sw, cudaStream_t st, const float4* L, const float4*
 template <class CP>
 cudaError_t preload_sweeps();
 template <class CP>
-void launch_heavy_scan(unsigned g, cudaStream_t st, const uint32_t* skeys, const int32_t* cstart,
+void launch_heavy_scan(unsigned g, cudaStream_t st, const float4* XP, const int32_t* cstart,
                        const int32_t* cend, uint32_t threshold, uint32_t n, CP cp, uint8_t* heavy,
                        uint32_t* list, uint32_t* count);
 template <class CP>
@@ -77,7 +77,7 @@ void launch_diagnostics(unsigned g, cudaStream_t st, const float4* P, const floa
                         const int32_t* cend, float4* out, uint32_t n, CP cp);
 
 template <class CP>
-void launch_highlight(unsigned g, cudaStream_t st, const uint32_t* skeys, const uint32_t* perm,
+void launch_highlight(unsigned g, cudaStream_t st, const float4* XP, const uint32_t* perm,
                       const int32_t* cstart, const int32_t* cend, uint32_t* flags, uint32_t n,
                       CP cp);
 

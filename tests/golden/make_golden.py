@@ -1,6 +1,8 @@
 """Generates the golden fixtures: outputs of the reference's own compute
 shaders (compiled as C++ from the reference checkout by oracle/ref_build.py)
-for one substep of each scene in pin_scenes.py.  Run here, where the
+for one substep of each scene in pin_scenes.py (with the end of the last
+occupied cell written, see ref_driver.cpp's pbfr_set_cell_fix; the scenes'
+dummy particles keep both boundary cells away from the fluid).  Run here, where the
 reference checkout exists; the fixtures then travel to machines that lack it.
 
     python tests/golden/make_golden.py
@@ -21,19 +23,26 @@ import pin_scenes  # noqa: E402
 
 
 def main():
-    manifest = {}
+    mpath = os.path.join(HERE, "manifest.json")
+    # entries of other generators (make_multistep.py) are kept
+    manifest = {k: v for k, v in json.load(open(mpath))["sha256"].items()
+                if not k.startswith("ref_") or k[4:-4] not in pin_scenes.CASES} \
+        if os.path.exists(mpath) else {}
+    manifest = {k: v for k, v in manifest.items() if os.path.exists(os.path.join(HERE, k))}
     for name in pin_scenes.CASES:
         p, x4, v4 = pin_scenes.make(name)
         hl_in = pin_scenes.highlight_flags(x4.shape[0])
-        r = oracle.ref_substep(p, x4, v4, highlight=hl_in)
+        # the last cell's end, which findcells never writes, is n (cell_fix=2):
+        # a fresh texture would give the last-cell dummy a negative run count
+        r = oracle.ref_substep(p, x4, v4, highlight=hl_in, cell_fix=2)
         path = os.path.join(HERE, f"ref_{name}.npz")
         np.savez_compressed(path, x_in=x4, v_in=v4, x=r["x"], v=r["v"], ids=r["ids"],
                             lam=r["lambda"], hl_in=hl_in, hl=r["highlight"])
         manifest[os.path.basename(path)] = hashlib.sha256(open(path, "rb").read()).hexdigest()
-    with open(os.path.join(HERE, "manifest.json"), "w") as f:
-        json.dump({"generator": "tests/golden/make_golden.py",
+    with open(mpath, "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py, tests/golden/make_multistep.py",
                    "source": "reference shaders compiled by oracle/ref_build.py",
-                   "sha256": manifest}, f, indent=1)
+                   "sha256": dict(sorted(manifest.items()))}, f, indent=1)
     print(json.dumps(manifest, indent=1))
 
 
