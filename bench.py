@@ -218,6 +218,50 @@ def batched_vs_plain(stream, num_scenes: int = 256, substeps: int = 100):
             "bit_identical_sampled_scenes": bool(same)}
 
 
+def batched_sharded(stream, rank: int, world: int, barrier, num_scenes: int = 256,
+                    substeps: int = 100):
+    """The 256-scene batch split across ranks by scene (scenes.shard_batch):
+    one batched handle per rank over its scenes, no collective on the data
+    path; the timed region (barrier and synchronise on both sides) is the
+    slowest rank's.  Whole-job scenes/s = num_scenes / that time."""
+    import torch
+    import torch.distributed as dist
+    import pbf_gb300 as pg
+    from pbf_gb300 import scenes
+    scs = scenes.batch_scenes(num_scenes, substeps=substeps)
+    mine, params, counts, x4, v4 = scenes.shard_batch(scs, rank, world)
+    b = pg.SPHBatch(params, counts) if mine else None
+    if b is not None:
+        b.set_stream(stream.cuda_stream)
+        b.set_state(x4, v4)
+        b.step(3)
+        b.set_state(x4, v4)
+    torch.cuda.synchronize()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    if b is not None:
+        b.step(substeps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    t = torch.tensor([e0.elapsed_time(e1)], device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    n_local = torch.tensor([float(x4.shape[0])], device="cuda")
+    if world > 1:
+        dist.all_reduce(n_local)
+    it = scs[0].params.num_solver_iterations
+    if b is not None:
+        b.close()
+    return {"scenes": num_scenes, "ranks": world, "scenes_on_rank0": len(mine) if rank == 0 else None,
+            "substeps": substeps, "ms": ms, "scenes_per_s": num_scenes / (ms * 1e-3),
+            "particle_iters_per_s": float(n_local.item()) * it * substeps / (ms * 1e-3),
+            "note": "scenes sharded by particle count (largest first); each rank one batched "
+                    "handle, no data-path collective; time = max over ranks"}
+
+
 def splat_leg(stream, reps: int = 20):
     """SurfaceReconstruction's particle passes (pbf_splat) on the reference's
     own scene (65,536 particles, after 20 substeps) and camera, at the
@@ -529,9 +573,12 @@ def _sig(x, digits: int = 4):
     return x
 
 
-def legs_summary(stable, full, batched, adjoint, adjoint5, small, recov) -> dict:
+def legs_summary(stable, full, batched, adjoint, adjoint5, small, recov, sharded=None) -> dict:
     """The headline figure of each leg (rounded to 4 digits)."""
     out = {}
+    if sharded:
+        out["batched_256_sharded"] = _sig({"ranks": sharded["ranks"],
+                                           "scenes_per_s": sharded["scenes_per_s"]})
     if full:
         out["full_500"] = _sig({"value": full["value"], "ms_per_step": full["ms_per_step"],
                                 "ms_per_step_by_100": full["ms_per_step_by_100"]})
@@ -750,6 +797,11 @@ def main():
         sim.close()
         torch.cuda.empty_cache()
         batched = batched_vs_plain(stream)
+    sharded = None
+    if world > 1:
+        sim.close()
+        torch.cuda.empty_cache()
+        sharded = batched_sharded(stream, rank, world, barrier)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -780,6 +832,7 @@ def main():
             "kernel_share": {k: v / total_stage for k, v in stages.items()},
             "gpu_launches": launches,
             "detail": {"stable_500": stable, "full_500": full, "batched_256": batched,
+                       "batched_256_sharded": sharded,
                        "adjoint_32k": adjoint, "adjoint_32k_epsilon_5": adjoint5,
                        "splat_reference_scene": splats, "dam_break_16k_200": small,
                        "recovery_64": recov, "state_after_window": state_after},
@@ -787,7 +840,7 @@ def main():
             "cpu_baseline": cpu,
             # compact figures of every leg, last on the line so that a
             # truncated tail of the output still shows them
-            "legs": legs_summary(stable, full, batched, adjoint, adjoint5, small, recov),
+            "legs": legs_summary(stable, full, batched, adjoint, adjoint5, small, recov, sharded),
         }
         print(json.dumps(line), flush=True)
     if world > 1:

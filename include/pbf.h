@@ -58,6 +58,9 @@ typedef enum pbf_status {
                                         reference's packed 8-bit count
                                         (shaders/sph/foreachneighbour.glsl:5) would have
                                         dropped it.  Informational only. */
+#define PBF_DEV_INDEX 0x8u           /* a bounds check of the bounds-checked build
+                                        (compiled with -DPBF_CHECK) failed; the access
+                                        was skipped */
 
 /* Where a caller pointer lives. */
 #define PBF_HOST 0
@@ -444,6 +447,13 @@ const char* pbf_status_string(pbf_status status);
  * `after`-th device allocation made by the library from now on (0 = the next
  * one) fails as out of memory, without reaching the device; negative disarms. */
 void pbf_debug_fail_allocation(int after);
+/* Device-side timeout test hook (no reference counterpart): with spins > 0,
+ * every radix-sort pass launched (or captured into a graph) after the call
+ * waits on a word nothing sets instead of its predecessor tile, gives up after
+ * `spins` polls and latches PBF_DEV_SORT_TIMEOUT; the sort's results are then
+ * invalid and the call that synchronises reports PBF_ERR_DEVICE_FAULT.  No
+ * wait is unbounded and every write stays in bounds.  0 disarms. */
+void pbf_debug_sort_stall(uint32_t spins);
 /* Message of the last failed call on `sim`, or of the last failed call
  * without a handle when sim is NULL.  Never NULL. */
 const char* pbf_last_error(const pbf_sim* sim);

@@ -22,6 +22,7 @@ PBF_ERR_UNSUPPORTED = 6
 PBF_DEV_NONFINITE = 0x1
 PBF_DEV_SORT_TIMEOUT = 0x2
 PBF_DEV_RUN_OVER_127 = 0x4
+PBF_DEV_INDEX = 0x8
 
 PBF_HOST = 0
 PBF_DEVICE = 1
@@ -160,11 +161,21 @@ SIGNATURES = {
     "pbf_release_record": (C.c_int, [_P]),
     "pbf_status_string": (C.c_char_p, [C.c_int]),
     "pbf_debug_fail_allocation": (None, [C.c_int]),
+    "pbf_debug_sort_stall": (None, [C.c_uint32]),
     "pbf_last_error": (C.c_char_p, [_P]),
     "pbf_abi_version": (C.c_int, []),
 }
 
 _lib = None
+
+
+def _bind(path: str) -> C.CDLL:
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
 
 
 def load() -> C.CDLL:
@@ -176,13 +187,20 @@ def load() -> C.CDLL:
         raise RuntimeError(
             f"{LIB_PATH} is missing: build it with `python -m pbf_gb300.build` "
             "(there is no CPU fallback)")
-    lib = C.CDLL(LIB_PATH)
-    for name, (res, args) in SIGNATURES.items():
-        fn = getattr(lib, name)
-        fn.restype = res
-        fn.argtypes = args
-    _lib = lib
-    return lib
+    _lib = _bind(LIB_PATH)
+    return _lib
+
+
+def load_checked() -> C.CDLL:
+    """Loads the bounds-checked build (-DPBF_CHECK,
+    pbf_gb300/_build_check/libpbf_gb300_check.so: index checks set
+    PBF_DEV_INDEX instead of faulting), a separate library with the same
+    entry points; build it with `python -m pbf_gb300.build --check`."""
+    from .build import CHECK_LIB
+    if not os.path.exists(CHECK_LIB):
+        raise RuntimeError(f"{CHECK_LIB} is missing: build it with "
+                           "`python -m pbf_gb300.build --check`")
+    return _bind(CHECK_LIB)
 
 
 class PbfError(RuntimeError):

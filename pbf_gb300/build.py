@@ -20,6 +20,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libpbf_gb300.so")
+# the bounds-checked variant (-DPBF_CHECK): index checks latch PBF_DEV_INDEX
+CHECK_BUILD = os.path.join(HERE, "_build_check")
+CHECK_LIB = os.path.join(CHECK_BUILD, "libpbf_gb300_check.so")
 ROOT = os.path.dirname(HERE)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -55,36 +58,42 @@ def _run(cmd: list[str]) -> None:
         raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
 
 
-def build(verbose: bool = False, jobs: int | None = None) -> str:
-    """Compiles and links the library if anything changed; returns its path."""
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose: bool = False, jobs: int | None = None, check: bool = False) -> str:
+    """Compiles and links the library if anything changed; returns its path.
+    check=True builds the bounds-checked variant (-DPBF_CHECK) instead, into
+    its own directory."""
+    out_dir, lib_path = (CHECK_BUILD, CHECK_LIB) if check else (BUILD, LIB)
+    defs = ["-DPBF_CHECK"] if check else []
+    os.makedirs(out_dir, exist_ok=True)
     nvcc = _nvcc()
     deps = _deps()
     jobs_list = []
     objs = []
     for src in sorted(glob.glob(os.path.join(CSRC, "*.cu"))):
-        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+        obj = os.path.join(out_dir, os.path.basename(src) + ".o")
         objs.append(obj)
         if _stale(obj, [src] + deps):
-            jobs_list.append([nvcc] + NVCC_FLAGS + ["-c", src, "-o", obj])
+            jobs_list.append([nvcc] + NVCC_FLAGS + defs + ["-c", src, "-o", obj])
     for src in sorted(glob.glob(os.path.join(CSRC, "*.cpp"))):
-        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+        obj = os.path.join(out_dir, os.path.basename(src) + ".o")
         objs.append(obj)
         if _stale(obj, [src] + deps):
-            jobs_list.append([os.environ.get("CXX", "g++")] + CXX_FLAGS + ["-c", src, "-o", obj])
+            jobs_list.append([os.environ.get("CXX", "g++")] + CXX_FLAGS + defs +
+                             ["-c", src, "-o", obj])
     if jobs_list:
         with ThreadPoolExecutor(max_workers=jobs or min(8, len(jobs_list))) as ex:
             for cmd, _ in zip(jobs_list, ex.map(_run, jobs_list)):
                 if verbose:
                     print(" ".join(cmd))
-    if jobs_list or _stale(LIB, objs):
-        tmp = LIB + ".tmp"
+    if jobs_list or _stale(lib_path, objs):
+        tmp = lib_path + ".tmp"
         _run([nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs)
-        os.replace(tmp, LIB)
+        os.replace(tmp, lib_path)
         if verbose:
-            print("linked", LIB)
-    return LIB
+            print("linked", lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":
-    print(build(verbose=True))
+    import sys
+    print(build(verbose=True, check="--check" in sys.argv))

@@ -144,7 +144,8 @@ struct AdjLists {
 };
 
 template <class F>
-__device__ __forceinline__ void adj_replay(uint32_t i, const AdjLists& al, F&& f) {
+__device__ __forceinline__ void adj_replay(uint32_t i, const DevConsts& c, const AdjLists& al,
+                                           F&& f) {
     const int32_t cnt = al.cnt[i];
     const uint32_t* p = al.idx + i;
     if (cnt > 0) {  // the next index is loaded one entry ahead
@@ -153,7 +154,7 @@ __device__ __forceinline__ void adj_replay(uint32_t i, const AdjLists& al, F&& f
         for (int32_t k = 0; k < cnt; ++k) {
             const uint32_t j = jn;
             if (k + 1 < cnt) jn = p[(size_t)(k + 1) * al.n];
-            f(j);
+            if (check_ok(c, j < c.n_total)) f(j);
         }
     }
 }
@@ -199,7 +200,7 @@ __device__ __forceinline__ void adj_scan_eval(uint32_t i, Ctr&& ctr, const DevCo
     }
     if (tot <= al.cap) {
         al.cnt[i] = (int32_t)tot;
-        adj_replay(i, al, f);
+        adj_replay(i, c, al, f);
     } else {
         al.cnt[i] = -1;
         visit_full(i, ctr, c, cstart, cend, f);
@@ -212,7 +213,7 @@ __device__ __forceinline__ void adj_visit_again(uint32_t i, Ctr&& ctr, const Dev
                                                 const int32_t* __restrict__ cend,
                                                 const AdjLists& al, F&& f) {
     if (al.cap && al.cnt[i] >= 0)
-        adj_replay(i, al, f);
+        adj_replay(i, c, al, f);
     else
         visit_full(i, ctr, c, cstart, cend, f);
 }

@@ -572,15 +572,26 @@ void invalidate_graph(pbf_sim* s) {
     }
 }
 
+// The bounds-checked build's fields of every scene's constants: the handle's
+// status word and particle count (make_consts leaves them empty).
+void bind_checks(pbf_sim* s) {
+    for (auto& c : s->sdc) {
+        c.check_status = s->status;
+        c.n_total = s->n;
+    }
+    if (!s->sdc.empty()) s->dc = s->sdc[0];
+}
+
 pbf_status check_status(pbf_sim* s) {
     PBF_CUDA(s, cudaMemcpyAsync(s->h_status, s->status, 2 * sizeof(uint32_t),
                                 cudaMemcpyDeviceToHost, s->stream));
     PBF_CUDA(s, cudaStreamSynchronize(s->stream));
     const uint32_t bits = s->h_status[0];
-    if (bits & (kDevNonFinite | kDevSortTimeout)) {
+    if (bits & (kDevNonFinite | kDevSortTimeout | kDevIndexFault)) {
         std::string m = "device status";
         if (bits & kDevNonFinite) m += ": non-finite position";
         if (bits & kDevSortTimeout) m += ": radix-sort lookback timed out";
+        if (bits & kDevIndexFault) m += ": index out of bounds (bounds-checked build)";
         return fail(s, PBF_ERR_DEVICE_FAULT, m);
     }
     if (s->h_status[1]) return fail(s, PBF_ERR_DEVICE_FAULT, "device status: cell key out of range");
@@ -668,6 +679,7 @@ pbf_status pbf_create_batch(const pbf_params* scene_params, const uint32_t* scen
         return st;
     }
     s->stream = s->own_stream;
+    bind_checks(s);
     reset_sweep_choice(s);
     e = num_scenes == 1 ? preload_sweeps<OneScene>() : preload_sweeps<ManyScenes>();
     if (e != cudaSuccess) {
@@ -732,10 +744,8 @@ pbf_status pbf_set_scene_params(pbf_sim* s, uint32_t scene, const pbf_params* p)
     s->sdc[scene] = make_consts(*p);
     s->sdc[scene].cell_base = base;
     apply_tuning(s->sdc[scene], *p, s->tuning);
-    if (scene == 0) {
-        s->params = *p;
-        s->dc = s->sdc[0];
-    }
+    bind_checks(s);
+    if (scene == 0) s->params = *p;
     if (s->nscenes > 1)
         PBF_CUDA(s, cudaMemcpy(s->d_consts + scene, &s->sdc[scene], sizeof(DevConsts),
                                cudaMemcpyHostToDevice));

@@ -20,6 +20,7 @@ constexpr int kBlock = 256;
 constexpr uint32_t kDevNonFinite = 0x1u;
 constexpr uint32_t kDevSortTimeout = 0x2u;
 constexpr uint32_t kDevRunOver127 = 0x4u;
+constexpr uint32_t kDevIndexFault = 0x8u;  // a bounds check of the -DPBF_CHECK build failed
 
 // Per-handle constants, folded on the host from pbf_params.
 struct DevConsts {
@@ -43,7 +44,24 @@ struct DevConsts {
     float r2list;        // inclusion threshold on |d|^2 at the predicted positions
     float margin_h;      // fixed part of the guard's rounding margin
     float wall_abs_max;  // largest |wall| coordinate (positions are clamped inside)
+    // bounds checks of the -DPBF_CHECK build: the handle's status word and
+    // its particle count (all scenes)
+    uint32_t* check_status;
+    uint32_t n_total;
 };
+
+// Index check of the bounds-checked build (-DPBF_CHECK): a failed check sets
+// kDevIndexFault in the handle's status word and the caller skips the access
+// (the next synchronising call reports PBF_ERR_DEVICE_FAULT).  In the normal
+// build the check is compiled out.
+#ifdef PBF_CHECK
+__device__ __forceinline__ bool check_ok(const DevConsts& c, bool ok) {
+    if (!ok) atomicOr(c.check_status, kDevIndexFault);
+    return ok;
+}
+#else
+__device__ __forceinline__ constexpr bool check_ok(const DevConsts&, bool) { return true; }
+#endif
 
 // Order-preserving neighbour lists of one substep.  idx is [cap][n] (entry k
 // of particle i at idx[k * n + i], coalesced across a warp); cnt[i] = -1

@@ -52,6 +52,9 @@ __device__ __forceinline__ void runs_of(int3 ctr, const DevConsts& c,
                 }
             }
         }
+        if (!check_ok(c, first == -1 || (first >= 0 && first <= last &&
+                                          (uint32_t)last <= c.n_total)))
+            first = -1;
         r.b[o] = first == -1 ? 0 : first;
         r.e[o] = first == -1 ? 0 : last;
     }
@@ -83,12 +86,22 @@ __device__ __forceinline__ void visit_full(uint32_t i, Ctr&& ctr, const DevConst
 // set by k_run_flags / k_find_cells.
 constexpr uint32_t kRunStride = 1024;
 
-// First run start after j (a set bit > j exists: the terminator at n).
-__device__ __forceinline__ uint32_t run_end(const uint32_t* __restrict__ runs, uint32_t j) {
+// First run start after j (a set bit > j exists: the terminator at n, and
+// one at every multiple of kRunStride, so the search reads at most
+// kRunStride / 32 + 1 words; the bounds-checked build enforces that).
+__device__ __forceinline__ uint32_t run_end(const DevConsts& c, const uint32_t* __restrict__ runs,
+                                           uint32_t j) {
     const uint32_t k = j + 1u;
     uint32_t w = k >> 5;
     uint32_t word = __ldg(runs + w) & (0xFFFFFFFFu << (k & 31u));
+#ifdef PBF_CHECK
+    for (uint32_t m = 0; word == 0u; ++m) {
+        if (!check_ok(c, m < kRunStride / 32u && w + 1u <= (c.n_total >> 5) + 1u)) return k;
+        word = __ldg(runs + ++w);
+    }
+#else
     while (word == 0u) word = __ldg(runs + ++w);
+#endif
     return (w << 5) + (uint32_t)(__ffs((int)word) - 1);
 }
 
@@ -136,6 +149,7 @@ __device__ __forceinline__ void visit_direct_piles(uint32_t i, Ctr&& ctr, const 
             const int32_t s = __ldg(cstart + cell);
             if (s == -1) continue;
             const int32_t t = __ldg(cend + cell);
+            if (!check_ok(c, s >= 0 && s <= t && (uint32_t)t <= c.n_total)) continue;
             if (t - s < kPileMin) {
                 if (b == -1) b = s;
                 e = t;
@@ -151,7 +165,7 @@ __device__ __forceinline__ void visit_direct_piles(uint32_t i, Ctr&& ctr, const 
                 if (in_run) {
                     const float3 d = sub3(pi, pos(j));
                     const float r2 = dot3(d, d);
-                    uint32_t r = run_end(runs, j);
+                    uint32_t r = run_end(c, runs, j);
                     if (r > (uint32_t)t) r = (uint32_t)t;
                     if (r2 == 0.0f) {
                         coincident(j, r, (r - j) - ((j <= i && i < r) ? 1u : 0u));

@@ -20,6 +20,7 @@
 #include "common.cuh"
 #include "internal.h"
 
+#include <atomic>
 #include <mutex>
 #include <string>
 
@@ -40,6 +41,12 @@ constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kValueMask = (1u << 30) - 1u;
 constexpr uint32_t kSpinLimit = 1u << 22;
+
+// Test hook (pbf_debug_sort_stall): when nonzero, every onesweep pass
+// launched afterwards looks back at a scratch word nothing sets, with this
+// spin limit, so each tile after the first gives up and latches
+// kDevSortTimeout: the timeout path runs without a real stall.
+std::atomic<uint32_t> g_stall_spins{0};
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
@@ -104,7 +111,7 @@ __global__ void __launch_bounds__(kSortThreads)
 k_onesweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
            uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n, uint32_t shift,
            uint32_t dmask, const uint32_t* __restrict__ digit_base, uint32_t* tile_status, uint32_t* tile_counter,
-           uint32_t* status) {
+           uint32_t* status, const uint32_t* stall_word, uint32_t spin_limit) {
     __shared__ uint32_t s_k[kTile];
     __shared__ uint32_t s_v[kTile];
     __shared__ uint32_t s_wh[kSortWarps][256];
@@ -177,11 +184,11 @@ k_onesweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
     if (tile > 0) {
         int64_t t = (int64_t)tile - 1;
         while (t >= 0) {
-            const uint32_t* ps = tile_status + (uint64_t)t * 256 + d;
+            const uint32_t* ps = stall_word ? stall_word : tile_status + (uint64_t)t * 256 + d;
             uint32_t s = load_volatile(ps);
             uint32_t spins = 0;
             while ((s & ~kValueMask) == 0u) {
-                if (++spins > kSpinLimit) {
+                if (++spins > spin_limit) {
                     atomicOr(status, kDevSortTimeout);
                     s = kFlagPrefix;  // give up: results are invalid, the status says so
                     break;
@@ -268,13 +275,16 @@ cudaError_t sort_pairs(const SortWorkspace& ws, const uint32_t* keys_in, uint32_
     // buffer it writes.
     const uint32_t* ksrc = keys_in;
     const uint32_t* vsrc = nullptr;
+    const uint32_t stall = g_stall_spins.load();
     for (uint32_t p = 0; p < passes; ++p) {
         const bool to_final = ((passes - 1 - p) % 2) == 0;
         uint32_t* kdst = to_final ? keys_out : ws.ktmp;
         uint32_t* vdst = to_final ? vals_out : ws.vtmp;
         k_onesweep<<<tiles, kSortThreads, 0, stream>>>(
             ksrc, vsrc, kdst, vdst, n, 8 * p, digit_mask(numbits, p), ws.hist + p * 256,
-            ws.tile_status + (size_t)p * 256 * ws.tiles_max, ws.counters + p * 32, status);
+            ws.tile_status + (size_t)p * 256 * ws.tiles_max, ws.counters + p * 32, status,
+            // a word of the pass's counter block that stays zero (only word 0 counts tiles)
+            stall ? ws.counters + p * 32 + 16 : nullptr, stall ? stall : kSpinLimit);
         ksrc = kdst;
         vsrc = vdst;
     }
@@ -282,6 +292,8 @@ cudaError_t sort_pairs(const SortWorkspace& ws, const uint32_t* keys_in, uint32_
 }
 
 }  // namespace pbf
+
+extern "C" void pbf_debug_sort_stall(uint32_t spins) { pbf::g_stall_spins.store(spins); }
 
 // ---- allocation-free variant -------------------------------------------------
 //

@@ -119,6 +119,12 @@ k_find_cells(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ pe
             atomicOr(status, kDevRunOver127);
     }
     float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#ifdef PBF_CHECK
+    if (valid && perm[i] >= n) {  // bounds-checked build: a bad permutation entry
+        atomicOr(status, kDevIndexFault);
+        return;
+    }
+#endif
     if (valid && P0) {
         p = __ldg(xstar + perm[i]);
         P0[i] = p;
@@ -159,9 +165,13 @@ k_find_cells(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ pe
 // visitors therefore produce the same sums, bit for bit.
 
 template <class F>
-__device__ __forceinline__ void visit_list(uint32_t i, int32_t cnt, const NbrLists& nl, F&& f) {
+__device__ __forceinline__ void visit_list(uint32_t i, const DevConsts& c, int32_t cnt,
+                                           const NbrLists& nl, F&& f) {
     const uint32_t* __restrict__ p = nl.idx + i;
-    for (int32_t k = 0; k < cnt; ++k) f(__ldg(p + (size_t)k * nl.n));
+    for (int32_t k = 0; k < cnt; ++k) {
+        const uint32_t j = __ldg(p + (size_t)k * nl.n);
+        if (check_ok(c, j < c.n_total)) f(j);
+    }
 }
 
 // Writer of particle i's exact pair list (PairLists): appends in visit order,
@@ -181,7 +191,8 @@ struct PairRecorder {
 
 // Replays particle i's exact pair list when one was recorded and fits.
 template <class F>
-__device__ __forceinline__ bool visit_pairs(uint32_t i, const PairLists& pl, F&& f) {
+__device__ __forceinline__ bool visit_pairs(uint32_t i, const DevConsts& c, const PairLists& pl,
+                                            F&& f) {
     if (!pl.cap) return false;
     const int32_t cnt = pl.cnt[i];
     if (cnt < 0) return false;
@@ -192,7 +203,7 @@ __device__ __forceinline__ bool visit_pairs(uint32_t i, const PairLists& pl, F&&
         for (int32_t k = 0; k < cnt; ++k) {
             const uint32_t j = jn;
             if (k + 1 < cnt) jn = __ldg(p + (size_t)(k + 1) * pl.n);
-            f(j);
+            if (check_ok(c, j < c.n_total)) f(j);
         }
     }
     return true;
@@ -452,14 +463,14 @@ k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
             listed = true;
             if constexpr (MODE == kPairs) {
                 PairRecorder rec{pw, i, 0u};
-                visit_list(i, cnt, nl, [&](uint32_t j) {
+                visit_list(i, c, cnt, nl, [&](uint32_t j) {
                     const float3 d = sub3(pi, xyz(__ldg(P + j)));
                     if (!(dot3(d, d) > c.r2cut)) rec(j);
                     eval(j);
                 });
                 rec.finish();
             } else {
-                visit_list(i, cnt, nl, eval);
+                visit_list(i, c, cnt, nl, eval);
             }
         }
     }
@@ -518,13 +529,13 @@ k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
         const float3 xi = xyz(XP[i]);
         auto ctr = [&] { return stencil_centre(XP[i], c); };  // neighbourcells.glsl:57
         bool done = false;
-        if constexpr (MODE == kPairs) done = visit_pairs(i, pr, body);
+        if constexpr (MODE == kPairs) done = visit_pairs(i, c, pr, body);
         if (!done) {
             bool listed = false;
             if constexpr (LISTS) {
                 const int32_t cnt = nl.cnt[i];
                 if (list_usable(c, nl, cnt, pi, xi, dmax_slot)) {
-                    visit_list(i, cnt, nl, body);
+                    visit_list(i, c, cnt, nl, body);
                     listed = true;
                 }
             }
@@ -852,6 +863,7 @@ k_commit(const float4* __restrict__ P, const uint32_t* __restrict__ perm, float4
     if (i >= n) return;
     const auto& c = cp.at(i);
     const uint32_t id = perm[i];
+    if (!check_ok(c, id < c.n_total)) return;
     const float4 q = P[i];
     const float4 xo = x[id];
     const float4 w = make_float4(fdiv(fsub(q.x, xo.x), c.dt), fdiv(fsub(q.y, xo.y), c.dt),
@@ -895,14 +907,14 @@ k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
             listed = true;
             if constexpr (MODE == kPairs) {
                 PairRecorder rec{pw, i, 0u};
-                visit_list(i, cnt, nl, [&](uint32_t j) {
+                visit_list(i, c, cnt, nl, [&](uint32_t j) {
                     const float3 d = sub3(pi, xyz(__ldg(P + j)));
                     if (!(dot3(d, d) > c.r2cut)) rec(j);
                     eval(j);
                 });
                 rec.finish();
             } else {
-                visit_list(i, cnt, nl, eval);
+                visit_list(i, c, cnt, nl, eval);
             }
         }
     }
@@ -965,13 +977,13 @@ k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ XP,
         eta = fma3(Qj.w, scale3(d, grad_scale(c.kg, c.h, len)), eta);  // :72
     };
     bool done = false;
-    if constexpr (MODE == kPairs) done = visit_pairs(i, pr, body);
+    if constexpr (MODE == kPairs) done = visit_pairs(i, c, pr, body);
     if (!done) {
         bool listed = false;
         if constexpr (LISTS) {
             const int32_t cnt = nl.cnt[i];
             if (list_usable(c, nl, cnt, pi, xyz(XP[i]), dmax_slot)) {
-                visit_list(i, cnt, nl, body);
+                visit_list(i, c, cnt, nl, body);
                 listed = true;
             }
         }
@@ -995,7 +1007,7 @@ k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ XP,
     const float l = fsqrt(dot3(eta, eta));  // :76
     if (l > 0.0f) eta = make_float3(fdiv(eta.x, l), fdiv(eta.y, l), fdiv(eta.z, l));  // :77-78
     const float3 vf = fma3(c.dteps, cross3(eta, xyz(OM[i])), xyz(VX[i]));  // :82
-    v[perm[i]] = make_float4(vf.x, vf.y, vf.z, 0.0f);                     // :85
+    if (check_ok(c, perm[i] < c.n_total)) v[perm[i]] = make_float4(vf.x, vf.y, vf.z, 0.0f);  // :85
 }
 
 // Per-particle density error |rho/rho0 - 1| (self excluded) and kinetic

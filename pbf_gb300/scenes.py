@@ -180,6 +180,19 @@ def shard(scenes_: list[Scene], rank: int, world: int) -> list[int]:
     return [k for k in range(len(scenes_)) if owner[k] == rank]
 
 
+def shard_batch(scenes_: list[Scene], rank: int, world: int):
+    """What one rank of a sharded batch steps: the indices of its scenes
+    (shard), their parameters and particle counts, and their initial states
+    concatenated in that order, the arguments of its own batched handle.
+    Scenes are independent, so nothing crosses ranks on the data path."""
+    idx = shard(scenes_, rank, world)
+    mine = [scenes_[k] for k in idx]
+    if not mine:
+        return idx, [], [], np.zeros((0, 4), np.float32), np.zeros((0, 4), np.float32)
+    x4, v4 = concat_state(mine)
+    return idx, [s.params for s in mine], [s.n for s in mine], x4, v4
+
+
 def reference_two_blocks(seed: int = 0) -> Scene:
     """The reference application's own scene (Simulation::ResetParticleBuffer,
     src/Simulation.cpp:206-246, with SPH's defaults, src/SPH.cpp:24-26,136-144):

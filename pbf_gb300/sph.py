@@ -48,8 +48,11 @@ def _as_f4(a, n: int) -> np.ndarray:
 class SPH:
     """One simulation handle (``pbf_sim``), the counterpart of ``SPH``."""
 
-    def __init__(self, numparticles: int, gridsize=(128, 64, 128), params: Params | None = None):
-        self._lib = load()
+    def __init__(self, numparticles: int, gridsize=(128, 64, 128), params: Params | None = None,
+                 lib=None):
+        # lib: another build of the library with the same entry points (the
+        # bounds-checked one, _capi.load_checked()); default the normal build
+        self._lib = lib if lib is not None else load()
         p = params.copy() if params is not None else default_params(gridsize)
         if params is not None and tuple(p.grid) != tuple(int(g) for g in gridsize):
             gridsize = tuple(p.grid)
@@ -397,8 +400,8 @@ class SPHBatch(SPH):
     bit-identically to the same scene in its own :class:`SPH`.
     """
 
-    def __init__(self, scene_params, scene_counts):
-        self._lib = load()
+    def __init__(self, scene_params, scene_counts, lib=None):
+        self._lib = lib if lib is not None else load()
         ps = list(scene_params)
         counts = [int(c) for c in scene_counts]
         if len(ps) != len(counts) or not ps:

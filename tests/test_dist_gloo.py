@@ -1,7 +1,8 @@
 """Multi-process (world size 2, gloo on 127.0.0.1) coverage of what
-bench.py --gpus N does across ranks: split independent scenes across ranks
-without any exchange on the data path, then take the max of the ranks'
-times.  Runs on CPU: each rank steps its shard with the oracle."""
+bench.py --gpus N does across ranks: split the batch's independent scenes
+across ranks (scenes.shard_batch, the arguments of each rank's batched
+handle) without any exchange on the data path, then take the max of the
+ranks' times.  Runs on CPU: each rank steps its shard with the oracle."""
 import os
 import socket
 
@@ -27,13 +28,17 @@ def _worker(rank, world, port, out):
         from pbf_gb300 import scenes
         scs = scenes.batch_scenes(8, seed=2, iterations=2, nmin=200, nmax=1200, box_min=12,
                                   box_max=16)
-        mine = scenes.shard(scs, rank, world)
+        # the rank's batched-handle arguments, as bench.py's sharded leg builds them
+        mine, params, counts, x4, v4 = scenes.shard_batch(scs, rank, world)
         sums = np.zeros(len(scs))
-        for k in mine:
-            o = oracle.Oracle(scs[k].params, scs[k].n, threads=1)
-            o.set_state(scs[k].x4, scs[k].v4)
+        off = 0
+        for k, p, c in zip(mine, params, counts):
+            o = oracle.Oracle(p, c, threads=1)
+            o.set_state(x4[off:off + c], v4[off:off + c])
+            off += c
             o.step(1)
             sums[k] = float(np.sum(o.get_state()[0][:, :3], dtype=np.float64))
+        assert off == x4.shape[0]
         t = torch.tensor([float(rank + 1)])
         dist.all_reduce(t, op=dist.ReduceOp.MAX)  # the bench's max over ranks
         owned = torch.zeros(len(scs))

@@ -5,20 +5,28 @@ final positions to those of the seed-B run; gradients with respect to 64
 random initial-velocity components and the four scalars (CFM epsilon,
 s_corr k, XSPH c, vorticity epsilon).
 
-Two FP64 references (tests/adjoint_32k.py): central differences of the FP64
-oracle twin (step 1e-3) and forward-mode dual numbers of the same twin
-(exact derivatives of that program).  The FP32 adjoint must agree with the
-dual-number gradients within 1e-3 relative (with a floor of 1e-3 of the
-largest component), at a horizon where the two FP64 references agree with
-each other:
-  - epsilon = 5 (the reference's default CFM epsilon, a stable run): all 64
-    substeps;
-  - epsilon = 0.01 (the workload's own, unstable: the gradient grows
-    ~100-300x per substep): 2 substeps.  Central differences at step 1e-3
-    agree with the dual numbers to 1e-6 on the velocity components over 2
-    substeps, to 3e-2 over 3 and not at all over 4 (the step leaves the
-    linear range); the s_corr k component already needs a step of 1e-5 at 2
-    substeps (measured: 1e-3 gives 12% truncation error, 1e-5 gives 1e-6).
+References (tests/adjoint_32k.py):
+  dual32  forward-mode dual numbers on the FP32 oracle's trajectory, which
+          is the GPU's own bit for bit: the exact derivative of the path the
+          adjoint differentiates;
+  dual64  the same on the FP64 twin's trajectory;
+  fd      central differences of the FP64 twin, step 1e-3.
+The FP32 adjoint must agree with the reference within 1e-3 relative (floor
+1e-3 of the largest component):
+  - with dual32 over all 64 substeps at epsilon = 5 (the reference's default
+    CFM epsilon);
+  - with dual64 and fd at the longest horizon where those two FP64
+    references agree with each other.  Over 64 substeps they do not (central
+    differences at step 1e-3 cross kinks of the piecewise-smooth map: wall
+    contacts, neighbour changes; measured 0.7 on the velocity components,
+    0.9 on the scalars), and an FP32 and an FP64 trajectory part as well, so
+    that comparison runs where both are meaningful;
+  - at the workload's epsilon = 0.01 (unstable: the gradient grows
+    ~100-300x per substep) over 2 substeps.  Central differences at step
+    1e-3 agree with the dual numbers to 1e-6 on the velocity components over
+    2 substeps, to 3e-2 over 3 and not at all over 4; the s_corr k component
+    needs a step of 1e-5 already at 2 substeps (1e-3 gives 12% truncation
+    error, 1e-5 gives 1e-6).
 """
 import numpy as np
 import pytest
@@ -29,9 +37,7 @@ from tests import adjoint_32k as A
 
 pytestmark = pytest.mark.gpu
 
-# central differences on a subset at the full horizon (each coordinate is
-# two full 64-substep FP64 runs); the dual numbers cover all 64 coordinates
-N_FD_LONG = 8
+EPS5_FP64_HORIZON = 16
 
 
 def gpu_grads(a, substeps, tgt, cs, every=8):
@@ -47,22 +53,30 @@ def gpu_grads(a, substeps, tgt, cs, every=8):
     return np.array([dv0[i, c] for i, c in cs] + list(np.asarray(g[0], np.float64)))
 
 
-def test_adjoint_32k_epsilon_5_all_64_substeps(gpu, oracle_mod):
+def test_adjoint_32k_epsilon_5_all_64_substeps_on_its_own_trajectory(gpu, oracle_mod):
     a, b = A.scene(5.0)
     S = 64
     cs = A.coords(a.n)
     tgt = A.target(oracle_mod, b, S)
     g = gpu_grads(a, S, tgt, cs)
     assert np.all(np.isfinite(g))
+    ref = A.dual_grads(oracle_mod, a, S, tgt, cs, fp32=True)
+    err = A.rel_err(g, ref)
+    assert err.max() < 1e-3, (err.max(), int(err.argmax()))
+
+
+def test_adjoint_32k_epsilon_5_against_fp64_references(gpu, oracle_mod):
+    a, b = A.scene(5.0)
+    S = EPS5_FP64_HORIZON
+    cs = A.coords(a.n)
+    tgt = A.target(oracle_mod, b, S)
+    g = gpu_grads(a, S, tgt, cs)
     dual = A.dual_grads(oracle_mod, a, S, tgt, cs)
+    fd = A.fd_grads(oracle_mod, a, S, tgt, cs)
+    assert A.rel_err(fd, dual).max() < 1e-3
     err = A.rel_err(g, dual)
     assert err.max() < 1e-3, (err.max(), int(err.argmax()))
-    sub = cs[:N_FD_LONG]
-    fd = A.fd_grads(oracle_mod, a, S, tgt, sub)
-    ref = np.concatenate([dual[:N_FD_LONG], dual[-4:]])
-    # the two FP64 references agree, and the GPU agrees with the differences
-    assert A.rel_err(fd, ref).max() < 1e-3
-    assert A.rel_err(np.concatenate([g[:N_FD_LONG], g[-4:]]), fd).max() < 1e-3
+    assert A.rel_err(g, fd).max() < 1e-3
 
 
 def test_adjoint_32k_epsilon_001_two_substeps(gpu, oracle_mod):
@@ -79,3 +93,4 @@ def test_adjoint_32k_epsilon_001_two_substeps(gpu, oracle_mod):
     assert A.rel_err(fd, dual).max() < 1e-3
     err = A.rel_err(g, dual)
     assert err.max() < 1e-3, (err.max(), int(err.argmax()))
+    assert A.rel_err(g, A.dual_grads(oracle_mod, a, S, tgt, cs, fp32=True)).max() < 1e-3

@@ -113,3 +113,29 @@ def test_find_cells_rejects_key_out_of_range(gpu):
     en = torch.empty(10, dtype=torch.int32, device="cuda")
     torch.cuda.synchronize()
     assert gpu.pbf_find_cells(keys.data_ptr(), 3, 10, st.data_ptr(), en.data_ptr(), None) == 1
+
+
+def test_sort_lookback_timeout_is_reported_not_hung(gpu):
+    """The onesweep lookback spin is bounded.  pbf_debug_sort_stall makes
+    every tile after the first wait on a word nothing sets; each wait gives up
+    after the given number of polls, the status word records it and the call
+    returns PBF_ERR_DEVICE_FAULT instead of hanging.  The context stays usable:
+    the next sort, disarmed, is exact."""
+    from pbf_gb300 import _capi
+    rng = np.random.default_rng(3)
+    keys = rng.integers(0, 1 << 20, 300_000, dtype=np.uint64).astype(np.uint32)  # 74 tiles
+    k = torch.from_numpy(keys.view(np.int32)).cuda()
+    ko = torch.empty_like(k)
+    po = torch.empty_like(k)
+    torch.cuda.synchronize()
+    try:
+        gpu.pbf_debug_sort_stall(1000)
+        st = gpu.pbf_radix_sort(k.data_ptr(), ko.data_ptr(), po.data_ptr(), keys.size, 20, None)
+    finally:
+        gpu.pbf_debug_sort_stall(0)
+    assert st == _capi.PBF_ERR_DEVICE_FAULT
+    assert b"timed out" in gpu.pbf_last_error(None)
+    st = gpu.pbf_radix_sort(k.data_ptr(), ko.data_ptr(), po.data_ptr(), keys.size, 20, None)
+    assert st == _capi.PBF_OK
+    assert np.array_equal(po.cpu().numpy().view(np.uint32),
+                          np.argsort(keys, kind="stable").astype(np.uint32))
