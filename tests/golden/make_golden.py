@@ -24,11 +24,10 @@ import pin_scenes  # noqa: E402
 
 def main():
     mpath = os.path.join(HERE, "manifest.json")
-    # entries of other generators (make_multistep.py) are kept
-    manifest = {k: v for k, v in json.load(open(mpath))["sha256"].items()
-                if not k.startswith("ref_") or k[4:-4] not in pin_scenes.CASES} \
-        if os.path.exists(mpath) else {}
-    manifest = {k: v for k, v in manifest.items() if os.path.exists(os.path.join(HERE, k))}
+    # other generators' entries (make_multistep.py, make_splat_golden.py) are kept
+    doc = json.load(open(mpath)) if os.path.exists(mpath) else {}
+    manifest = {k: v for k, v in doc.get("sha256", {}).items()
+                if k[4:-4] not in pin_scenes.CASES and os.path.exists(os.path.join(HERE, k))}
     for name in pin_scenes.CASES:
         p, x4, v4 = pin_scenes.make(name)
         hl_in = pin_scenes.highlight_flags(x4.shape[0])
@@ -39,10 +38,11 @@ def main():
         np.savez_compressed(path, x_in=x4, v_in=v4, x=r["x"], v=r["v"], ids=r["ids"],
                             lam=r["lambda"], hl_in=hl_in, hl=r["highlight"])
         manifest[os.path.basename(path)] = hashlib.sha256(open(path, "rb").read()).hexdigest()
+    doc["generator"] = "tests/golden/make_golden.py, tests/golden/make_multistep.py"
+    doc["source"] = "reference shaders compiled by oracle/ref_build.py"
+    doc["sha256"] = dict(sorted(manifest.items()))
     with open(mpath, "w") as f:
-        json.dump({"generator": "tests/golden/make_golden.py, tests/golden/make_multistep.py",
-                   "source": "reference shaders compiled by oracle/ref_build.py",
-                   "sha256": dict(sorted(manifest.items()))}, f, indent=1)
+        json.dump(doc, f, indent=1)
     print(json.dumps(manifest, indent=1))
 
 
