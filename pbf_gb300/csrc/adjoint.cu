@@ -7,12 +7,19 @@
 // r = h, so freezing them gives the exact derivative almost everywhere.  The
 // wall clamp contributes its subgradient (zero along a clamped component).
 //
-// Every reverse sweep is written as a gather, not a scatter: the neighbour
-// relation is symmetric (candidates come from the 27-cell stencil, and the
-// in-range test depends on |p_i - p_j| only), and the pair functions obey
-// G(-d) = -G(d), H(-d) = H(d), W(-d) = W(d), so each particle sums the
-// contributions of its own equation and of its neighbours' equations from
-// per-particle adjoint quantities.  No atomics: results are deterministic.
+// Every reverse sweep is written as a gather, not a scatter: the pair
+// functions obey G(-d) = -G(d), H(-d) = H(d), W(-d) = W(d), so each particle
+// sums the contributions of its own equation and of its neighbours'
+// equations from per-particle adjoint quantities.  No atomics: results are
+// deterministic.  The candidate relation is symmetric except around particles
+// predicted outside the grid: the forward centres a stencil on the unclamped
+// predicted cell (neighbourcells.glsl:57) while the sort files the particle
+// under its clamped cell, so such a particle i may be a candidate of j without
+// j being one of i's.  The reverse sweeps therefore visit the stencil around
+// the clamped (key) cell, which holds both directions, and, in a substep with
+// such particles, weigh each pair's terms by two flags: `own` (j is i's
+// candidate: the terms of i's equation) and `trans` (i is j's candidate: the
+// terms of j's equation).
 //
 // Notation (sorted particle i, neighbour j, d = p_i - p_j, r = |d|):
 //   W(r)  = k6 (h^2 - r^2)^3                 poly6 (calclambda.glsl:41-47)
@@ -64,6 +71,8 @@ struct Tape {
     float4 *VSB = nullptr, *ETB = nullptr, *OMB = nullptr, *VCB = nullptr;  // sorted
     float4 *XSB = nullptr, *XOB = nullptr;  // x*-bar and x_old-bar (id order)
     double* acc = nullptr;                  // [kParams][n] per-particle parameter gradients (id order)
+    uint8_t* irr = nullptr;                 // [n] stencil centre != key cell (sorted), per substep
+    uint32_t* any_irr = nullptr;            // whether any particle of the substep is so
     std::vector<void*> owned;
 };
 
@@ -125,6 +134,34 @@ __device__ __forceinline__ float3 clamp_mask(float3 g, float3 p, const DevConsts
     if (p.z == c.lo[2] || p.z == c.hi[2]) g.z = 0.0f;
     return g;
 }
+
+// ---- candidate directions ---------------------------------------------------------
+
+// The key (sorted) cell of a predicted position, the clamped counterpart of
+// stencil_centre (counting.glsl:55 with the cap at G - 1).
+__device__ __forceinline__ int3 key_cell(float4 q, const DevConsts& c) {
+    return make_int3((int)cell_coord(q.x, c.G[0], c.Gi[0]), (int)cell_coord(q.y, c.G[1], c.Gi[1]),
+                     (int)cell_coord(q.z, c.G[2], c.Gi[2]));
+}
+
+// Whether each direction of pair (i, j) is a forward candidate (see the top
+// of this file).  `on` (the substep has irregular particles) is uniform.
+struct PairDirs {
+    const uint8_t* irr;
+    const float4* XPc;
+    const uint32_t* any;  // nonzero when the substep has irregular particles
+    __device__ __forceinline__ void of(const DevConsts& c, uint32_t i, uint32_t j, float& own,
+                                       float& trans) const {
+        own = trans = 1.0f;
+        if (!__ldg(any) || !(__ldg(irr + i) | __ldg(irr + j))) return;
+        const float4 qi = __ldg(XPc + i), qj = __ldg(XPc + j);
+        auto inside = [](int3 cell, int3 ctr) {
+            return abs(cell.x - ctr.x) <= 1 && abs(cell.y - ctr.y) <= 1 && abs(cell.z - ctr.z) <= 1;
+        };
+        own = inside(key_cell(qj, c), stencil_centre(qi, c)) ? 1.0f : 0.0f;
+        trans = inside(key_cell(qi, c), stencil_centre(qj, c)) ? 1.0f : 0.0f;
+    }
+};
 
 // ---- neighbour visits of the reverse sweeps -----------------------------------
 //
@@ -226,6 +263,22 @@ __device__ __forceinline__ const DevConsts& consts_of(const CP& cp, uint32_t id)
 
 // ---- reverse kernels --------------------------------------------------------------
 
+// Per substep: irr[i] = 1 when particle i's stencil centre is not its key
+// cell (predicted outside the grid); *any set when some particle is.
+template <class CP>
+__global__ void __launch_bounds__(kAdjBlock)
+k_adj_flags(const uint32_t* __restrict__ perm, const float4* __restrict__ XPc,
+            uint8_t* __restrict__ irr, uint32_t* __restrict__ any, uint32_t n, CP cp) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const DevConsts& c = consts_of(cp, perm[i]);
+    const int3 a = stencil_centre(XPc[i], c), b = key_cell(XPc[i], c);
+    const bool odd = a.x != b.x || a.y != b.y || a.z != b.z;
+    irr[i] = odd ? 1 : 0;
+    if (odd) atomicOr(any, 1u);
+}
+
+
 // vorticity.glsl:76-85 reversed, pointwise: from vf-bar to vs-bar, eta-bar and
 // the direct part of w-bar; accumulates d/d(eps_v).
 template <class CP>
@@ -264,7 +317,7 @@ k_adj_vort_b2(const uint32_t* __restrict__ perm, const float4* __restrict__ XPc,
               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
               const float4* __restrict__ Q, const float4* __restrict__ OM,
               const float4* __restrict__ ETB, float4* __restrict__ OMB, float4* __restrict__ PA,
-              AdjLists al, uint32_t n, CP cp) {
+              AdjLists al, PairDirs dirs, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t id = perm[i];
@@ -275,15 +328,17 @@ k_adj_vort_b2(const uint32_t* __restrict__ perm, const float4* __restrict__ XPc,
     const float3 ebi = f3(ETB[i]);
     float mb = 0.0f;
     float3 pb = make_float3(0.0f, 0.0f, 0.0f);
-    adj_scan_eval(i, [&] { return stencil_centre(XPc[i], c); }, c, cstart, cend, Q, pi, al, [&](uint32_t j) {
+    adj_scan_eval(i, [&] { return key_cell(XPc[i], c); }, c, cstart, cend, Q, pi, al, [&](uint32_t j) {
         const float4 Qj = __ldg(Q + j);
         const float3 d = pi - f3(Qj);
         const float r2 = dotf(d, d);
         if (r2 > c.r2cut || r2 == 0.0f) return;
         const Spiky sp(c, sqrtf(r2));
-        const float3 ebj = f3(__ldg(ETB + j));
+        float own, trans;
+        dirs.of(c, i, j, own, trans);
+        const float3 ebj = trans * f3(__ldg(ETB + j));
         mb -= dotf(ebj, sp.G(d));
-        pb = pb + sp.H(d, Qj.w * ebi - mi * ebj);
+        pb = pb + sp.H(d, (own * Qj.w) * ebi - mi * ebj);
     });
     float3 wb = f3(OMB[i]);
     if (mi > 0.0f) wb = wb + (mb / mi) * f3(OM[i]);
@@ -300,7 +355,7 @@ k_adj_vort_a(const uint32_t* __restrict__ perm, const float4* __restrict__ XPc,
              const float4* __restrict__ PF, const float4* __restrict__ VS,
              const float4* __restrict__ VSB, const float4* __restrict__ OMB,
              float4* __restrict__ VCB, float4* __restrict__ PA, double* __restrict__ acc_c,
-             AdjLists al, uint32_t n, CP cp) {
+             AdjLists al, PairDirs dirs, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t id = perm[i];
@@ -312,19 +367,22 @@ k_adj_vort_a(const uint32_t* __restrict__ perm, const float4* __restrict__ XPc,
     float3 vb = sbi;
     float3 pb = f3(PA[i]);
     float3 wsum = make_float3(0.0f, 0.0f, 0.0f);
-    adj_visit_again(i, [&] { return stencil_centre(XPc[i], c); }, c, cstart, cend, al, [&](uint32_t j) {
+    adj_visit_again(i, [&] { return key_cell(XPc[i], c); }, c, cstart, cend, al, [&](uint32_t j) {
         const float3 d = pi - f3(__ldg(PF + j));
         const float r2 = dotf(d, d);
         if (r2 > c.r2cut) return;
+        float own, trans;
+        dirs.of(c, i, j, own, trans);
         const float3 vji = f3(__ldg(VS + j)) - vi;
-        const float3 sbj = f3(__ldg(VSB + j));
+        const float3 sbj = trans * f3(__ldg(VSB + j));
+        const float3 sbo = own * sbi;
         const float W = w6(c, r2);
-        vb = vb + (c.cx * W) * (sbj - sbi);
-        wsum = wsum + W * vji;
-        pb = pb + (c.cx * dotf(sbi - sbj, vji)) * w6_grad(c, d, r2);
+        vb = vb + (c.cx * W) * (sbj - sbo);
+        wsum = wsum + (own * W) * vji;
+        pb = pb + (c.cx * dotf(sbo - sbj, vji)) * w6_grad(c, d, r2);
         if (r2 == 0.0f) return;
         const Spiky sp(c, sqrtf(r2));
-        const float3 wbs = wbi + f3(__ldg(OMB + j));
+        const float3 wbs = own * wbi + trans * f3(__ldg(OMB + j));
         vb = vb - crossf(sp.G(d), wbs);
         pb = pb + sp.H(d, crossf(wbs, vji));
     });
@@ -369,8 +427,8 @@ k_adj_delta_p(const uint32_t* __restrict__ perm, const float4* __restrict__ XPc,
               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
               const float4* __restrict__ L, const float4* __restrict__ AUX,
               const float4* __restrict__ QB, float4* __restrict__ PDB, float4* __restrict__ RS,
-              double* __restrict__ acc_eps, double* __restrict__ acc_k, AdjLists al, uint32_t n,
-              CP cp) {
+              double* __restrict__ acc_eps, double* __restrict__ acc_k, AdjLists al,
+              PairDirs dirs, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t id = perm[i];
@@ -382,7 +440,7 @@ k_adj_delta_p(const uint32_t* __restrict__ perm, const float4* __restrict__ XPc,
     float lb = 0.0f, kb = 0.0f;
     float3 pb = qbi;
     const float sc4 = c.scale * c.scale * c.scale * c.scale;
-    adj_scan_eval(i, [&] { return stencil_centre(XPc[i], c); }, c, cstart, cend, L, pi, al, [&](uint32_t j) {
+    adj_scan_eval(i, [&] { return key_cell(XPc[i], c); }, c, cstart, cend, L, pi, al, [&](uint32_t j) {
         const float4 Lj = __ldg(L + j);
         const float3 d = pi - f3(Lj);
         const float r2 = dotf(d, d);
@@ -394,13 +452,15 @@ k_adj_delta_p(const uint32_t* __restrict__ perm, const float4* __restrict__ XPc,
         const float s = c.negk * sc4 * W3 * W;
         const float a = (li + Lj.w + s) * c.oorho;
         const float3 G = sp.G(d);
-        const float3 dq = qbi - f3(__ldg(QB + j));
+        float own, trans;
+        dirs.of(c, i, j, own, trans);
+        const float3 dq = own * qbi - trans * f3(__ldg(QB + j));
         const float dqG = dotf(dq, G);
         lb += c.oorho * dqG;
         // (ds/dr)/r = 4 negk scale^4 W^3 (-6 k6 (h^2 - r^2)^2)
         const float sr = 4.0f * c.negk * sc4 * W3 * (-6.0f * c.k6 * t * t);
         pb = pb + sp.H(d, a * dq) + (c.oorho * sr * dqG) * d;
-        kb -= c.oorho * dotf(qbi, G) * sc4 * W3 * W;
+        kb -= own * c.oorho * dotf(qbi, G) * sc4 * W3 * W;
     });
     const float4 aux = AUX[i];
     const float D = aux.w + c.eps;
@@ -421,8 +481,8 @@ k_adj_lambda(const uint32_t* __restrict__ perm, const float4* __restrict__ XPc,
              const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
              const float4* __restrict__ L, const float4* __restrict__ AUX,
              const float4* __restrict__ RS, const float4* __restrict__ PDB,
-             float4* __restrict__ QB, float4* __restrict__ XSB, int first, AdjLists al, uint32_t n,
-             CP cp) {
+             float4* __restrict__ QB, float4* __restrict__ XSB, int first, AdjLists al,
+             PairDirs dirs, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t id = perm[i];
@@ -431,17 +491,19 @@ k_adj_lambda(const uint32_t* __restrict__ perm, const float4* __restrict__ XPc,
     const float4 RSi = RS[i];
     const float3 gi = f3(AUX[i]);
     float3 pb = f3(PDB[i]);
-    adj_visit_again(i, [&] { return stencil_centre(XPc[i], c); }, c, cstart, cend, al, [&](uint32_t j) {
+    adj_visit_again(i, [&] { return key_cell(XPc[i], c); }, c, cstart, cend, al, [&](uint32_t j) {
         const float3 d = pi - f3(__ldg(L + j));
         const float r2 = dotf(d, d);
         if (r2 > c.r2cut) return;
+        float own, trans;
+        dirs.of(c, i, j, own, trans);
         const float4 RSj = __ldg(RS + j);
-        pb = pb + (RSi.x + RSj.x) * w6_grad(c, d, r2);
+        pb = pb + (own * RSi.x + trans * RSj.x) * w6_grad(c, d, r2);
         if (r2 == 0.0f) return;
         const Spiky sp(c, sqrtf(r2));
         const float3 gij = c.oorho * sp.G(d);
         const float3 gj = f3(__ldg(AUX + j));
-        const float3 u = RSi.y * (gij + gi) + RSj.y * (gij - gj);
+        const float3 u = (own * RSi.y) * (gij + gi) + (trans * RSj.y) * (gij - gj);
         pb = pb + (2.0f * c.oorho) * sp.H(d, u);
     });
     if (first) {
@@ -511,6 +573,8 @@ cudaError_t alloc_tape(pbf_sim* s, Tape* t) {
     for (float4** w : work)
         if (e == cudaSuccess) e = talloc(t, w, n);
     if (e == cudaSuccess) e = talloc(t, &t->acc, (size_t)kParams * n);
+    if (e == cudaSuccess) e = talloc(t, &t->irr, n);
+    if (e == cudaSuccess) e = talloc(t, &t->any_irr, 1);
     return e;
 }
 
@@ -525,23 +589,31 @@ cudaError_t reverse_substep(pbf_sim* s, Tape* t, const Tape::Slot& sl, const CP&
     double* acc_c = t->acc + 2 * (size_t)n;
     double* acc_ev = t->acc + 3 * (size_t)n;
     const AdjLists al{s->pair_idx, s->pair_cnt, s->pair_cap, n};
+    // the substep's predicted positions (sorted), where every stencil is
+    // centred (neighbourcells.glsl:57): the first lambda sweep's L holds them,
+    // and PF does when there is no solver iteration
+    const float4* XPc = iters > 0 ? sl.L[0] : sl.PF;
+    cudaError_t fe = cudaMemsetAsync(t->any_irr, 0, sizeof(uint32_t), st);
+    if (fe != cudaSuccess) return fe;
+    k_adj_flags<<<g, kAdjBlock, 0, st>>>(sl.perm, XPc, t->irr, t->any_irr, n, cp);
+    const PairDirs dirs{t->irr, XPc, t->any_irr};
     if (t->vort) {
         k_adj_vort_b1<<<g, kAdjBlock, 0, st>>>(sl.perm, t->VB, sl.OM, sl.ETA, t->VSB, t->ETB,
                                                t->OMB, acc_ev, n, cp);
-        k_adj_vort_b2<<<g, kAdjBlock, 0, st>>>(sl.perm, sl.PF, sl.cstart, sl.cend, sl.Q, sl.OM,
-                                               t->ETB, t->OMB, t->PA, al, n, cp);
-        k_adj_vort_a<<<g, kAdjBlock, 0, st>>>(sl.perm, sl.PF, sl.cstart, sl.cend, sl.PF, sl.VS,
-                                              t->VSB, t->OMB, t->VCB, t->PA, acc_c, al, n, cp);
+        k_adj_vort_b2<<<g, kAdjBlock, 0, st>>>(sl.perm, XPc, sl.cstart, sl.cend, sl.Q, sl.OM,
+                                               t->ETB, t->OMB, t->PA, al, dirs, n, cp);
+        k_adj_vort_a<<<g, kAdjBlock, 0, st>>>(sl.perm, XPc, sl.cstart, sl.cend, sl.PF, sl.VS,
+                                              t->VSB, t->OMB, t->VCB, t->PA, acc_c, al, dirs, n, cp);
     }
     k_adj_commit<<<g, kAdjBlock, 0, st>>>(sl.perm, t->XB, t->VB, t->VCB, t->PA, sl.PF, t->QB,
                                           t->XOB, t->XSB, t->vort ? 1 : 0, iters, n, cp);
     for (int k = iters - 1; k >= 0; --k) {
-        k_adj_delta_p<<<g, kAdjBlock, 0, st>>>(sl.perm, sl.PF, sl.cstart, sl.cend, sl.L[k],
+        k_adj_delta_p<<<g, kAdjBlock, 0, st>>>(sl.perm, XPc, sl.cstart, sl.cend, sl.L[k],
                                                sl.AUX[k], t->QB, t->PDB, t->RS, acc_eps, acc_k, al,
-                                               n, cp);
-        k_adj_lambda<<<g, kAdjBlock, 0, st>>>(sl.perm, sl.PF, sl.cstart, sl.cend, sl.L[k],
+                                               dirs, n, cp);
+        k_adj_lambda<<<g, kAdjBlock, 0, st>>>(sl.perm, XPc, sl.cstart, sl.cend, sl.L[k],
                                               sl.AUX[k], t->RS, t->PDB, t->QB, t->XSB,
-                                              k == 0 ? 1 : 0, al, n, cp);
+                                              k == 0 ? 1 : 0, al, dirs, n, cp);
     }
     k_adj_predict<<<g, kAdjBlock, 0, st>>>(t->XSB, t->XOB, t->XB2, t->VB2, n, cp);
     std::swap(t->XB, t->XB2);

@@ -194,3 +194,30 @@ def test_batched_adjoint_matches_single_scenes(gpu):
         assert np.allclose(bdv[sl], dv0, rtol=1e-6, atol=1e-9)
         assert np.allclose(bdx[sl], dx0, rtol=1e-6, atol=1e-9)
         assert np.allclose(bg[k], g, rtol=1e-6, atol=1e-12)
+
+
+def test_adjoint_with_stencils_outside_the_grid(gpu, oracle_mod):
+    """Particles predicted below the floor centre their stencil outside the
+    grid (neighbourcells.glsl:57), so they may be candidates of a neighbour
+    that is not one of theirs.  The reverse sweeps weigh each pair's two
+    directions separately; the adjoint must match the exact derivative of the
+    same FP32 trajectory (dual numbers on the FP32 oracle) within 1e-3."""
+    import sys
+    import os
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import pin_scenes
+    p, x4, v4 = pin_scenes.make("h1_eps5_below_floor")
+    n = x4.shape[0]
+    S = 2
+    rng = np.random.default_rng(5)
+    w = rng.normal(size=(n, 4)).astype(np.float32)
+    w[:, 3] = 0
+    dx0, dv0, gp, _ = gpu_grads(p, x4, v4, S, w, np.zeros_like(w), every=1)
+    low = np.flatnonzero(v4[:, 1] < -150)[:6]  # predicted below y = -1 in the first substep
+    coords = [(int(i), 1) for i in low] + [(int(rng.integers(n)), int(rng.integers(3))) for _ in range(6)]
+    dirs = [("v", i, c) for i, c in coords] + [("x", i, c) for i, c in coords[:4]]
+    dirs += [(nm,) for nm in PARAMS]
+    x, _, xd, _ = oracle_mod.dual_tangents(p, x4, v4, S, dirs, fp32=True)
+    ref = np.einsum("nc,knc->k", w[:, :3].astype(np.float64), xd)
+    g = [dv0[i, c] for i, c in coords] + [dx0[i, c] for i, c in coords[:4]] + list(gp)
+    check(g, ref, "gradients with stencils outside the grid")

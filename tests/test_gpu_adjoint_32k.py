@@ -38,6 +38,7 @@ from tests import adjoint_32k as A
 pytestmark = pytest.mark.gpu
 
 EPS5_FP64_HORIZON = 16
+N_FD = 16
 
 
 def gpu_grads(a, substeps, tgt, cs, every=8):
@@ -72,11 +73,14 @@ def test_adjoint_32k_epsilon_5_against_fp64_references(gpu, oracle_mod):
     tgt = A.target(oracle_mod, b, S)
     g = gpu_grads(a, S, tgt, cs)
     dual = A.dual_grads(oracle_mod, a, S, tgt, cs)
-    fd = A.fd_grads(oracle_mod, a, S, tgt, cs)
-    assert A.rel_err(fd, dual).max() < 1e-3
+    # central differences on the first N_FD coordinates and the scalars (two
+    # full FP64 runs each); the dual numbers cover all 64
+    fd = A.fd_grads(oracle_mod, a, S, tgt, cs[:N_FD])
+    sub = np.r_[0:N_FD, len(cs):len(cs) + 4]
+    assert A.rel_err(fd, dual[sub]).max() < 1e-3
     err = A.rel_err(g, dual)
     assert err.max() < 1e-3, (err.max(), int(err.argmax()))
-    assert A.rel_err(g, fd).max() < 1e-3
+    assert A.rel_err(g[sub], fd).max() < 1e-3
 
 
 def test_adjoint_32k_epsilon_001_two_substeps(gpu, oracle_mod):

@@ -49,14 +49,17 @@ def test_corner_piles_bit_exact(gpu, piled, tuning):
 
 def test_run_flag_clear_while_calm(gpu):
     """Near rest density (8 particles per cell) no 3-cell run reaches 128:
-    the informational bit stays clear, so the packed form would agree (in
+    the informational bit stays clear, so the packed form would agree.  In
     the oracle's sort the first window of 128 particles within three cells
-    appears at substep 25)."""
+    appears at substep 8 of the 16,384-particle dam break, and the bit sets
+    there."""
     sc = scenes.plain_16k()
     g = pg.SPH(sc.n, tuple(sc.params.grid), sc.params)
     g.set_state(sc.x4, sc.v4)
-    g.step(10)
+    g.step(7)
     assert g.device_status() & pg.PBF_DEV_RUN_OVER_127 == 0
+    g.step(1)
+    assert g.device_status() & pg.PBF_DEV_RUN_OVER_127
 
 
 def test_corner_piles_in_a_batch(gpu, oracle_mod):
