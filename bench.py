@@ -822,7 +822,12 @@ def main():
                     "ms_per_step": e2e_ms / E, "steps": E},
             "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[dom], "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "alg_bytes_per_launch": ALG_BYTES[dom] * scene.n,
+                         "traffic": traffic,
+                         "traffic_source": (None if traffic is None else
+                                            f"{prof.get('source')} (ncu capture at commit "
+                                            f"{prof.get('commit', 'unknown')}; per launch, scaled "
+                                            f"by particles)"),
+                         "alg_bytes_per_launch": ALG_BYTES[dom] * scene.n,
                          "ms_per_launch": per_launch[dom],
                          "issue_active": (prof or {}).get("issue_active", {}).get(dom),
                          "note": "neighbour sweeps are bound by instruction issue (issue_active: "

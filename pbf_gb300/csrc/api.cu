@@ -317,12 +317,14 @@ uint32_t kernels_per_substep(const pbf_sim* s) {
     const bool vort = s->params.vorticity_confinement != 0;
     uint32_t k = 1u /*predict*/ + 1u /*unmark*/ + 2u + passes /*sort*/ + 1u /*cells*/ +
                  2u * iters + 1u /*commit*/ + (vort ? 2u : 0u);
-    {  // run-start bits after each delta-p whose positions a direct sweep reads next
+    {  // run-start bits before each direct sweep (enqueue_impl): the positions
+       // of every lambda sweep after the first, (p, lambda) of every delta-p,
+       // (p, v) and (p, |vorticity|) of the vorticity passes
         const PassModes a = modes_of(s, s->pass_solver), b = modes_of(s, s->pass_vort);
         const bool lists = skin_lists_on(s);
-        const bool rs = !lists && (a.first == 0 || a.second == 0);
-        const bool rv = !lists && vort && (b.first == 0 || b.second == 0);
-        if (iters > 0) k += (iters - 1) * (rs ? 1u : 0u) + (rv ? 1u : 0u);
+        if (!lists && iters > 0) k += (iters - 1) * (a.first == 0 ? 1u : 0u);
+        if (!lists) k += iters * (a.second == 0 ? 1u : 0u);
+        if (!lists && vort) k += (b.first == 0 ? 1u : 0u) + (b.second == 0 ? 1u : 0u);
     }
     if (mixed_on(s)) {  // the flag pass and a cooperative launch after each one-thread sweep
         const PassModes a = modes_of(s, s->pass_solver), b = modes_of(s, s->pass_vort);
@@ -498,9 +500,15 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
     // also records the neighbour lists the later sweeps replay.
     const NbrLists nl{s->nbr_idx, s->nbr_cnt, s->guard, s->nbr_cap, n};
     // the direct sweeps skip runs of coincident candidates (neighbours.cuh:
-    // visit_direct_piles); run-start bits of each position set they read
-    const bool runs_solver = !lists && (ms.first == 0 || ms.second == 0);
-    const bool runs_vort = !lists && vort && (mv.first == 0 || mv.second == 0);
+    // visit_direct_piles); run-start bits of each position set they read, and
+    // for delta-p and the vorticity passes over their other inputs as well
+    // (lambda, the committed velocity, |vorticity|), so that a run's terms
+    // are all equal (k_run_flags_vals)
+    const bool lam_direct = !lists && ms.first == 0, dp_direct = !lists && ms.second == 0;
+    const bool va_direct = !lists && vort && mv.first == 0;
+    const bool vb_direct = !lists && vort && mv.second == 0;
+    const bool runs_solver = lam_direct || dp_direct;
+    const bool runs_vort = va_direct || vb_direct;
     const PairLists pl{s->pair_idx, s->pair_cnt, s->pair_cap, n, mixed ? s->heavy : nullptr,
                        s->heavy_list, s->heavy_count,
                        runs_solver || runs_vort ? s->runs : nullptr};
@@ -521,13 +529,15 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
         else
             launch_lambda(s_lam, st, cur, s->XP, s->skeys, s->cstart, s->cend, Lk, aux, nl, pl,
                           scan_set(cur_set), in_slot, n, cps);
+        if (dp_direct)
+            k_run_flags_vals<<<grid_for(n + 1), kBlock, 0, st>>>(Lk, nullptr, 1, n, s->runs);
         mark(4 + 2 * it);
         // delta-p replays the pair lists the lambda sweep just recorded
         const bool write_scan = it + 1 < iters ? solver_scans : vort_scans;
         launch_delta_p(s_dp, st, Lk, s->XP, s->skeys, s->cstart, s->cend, nxt, nl, pl,
                        scan_set(cur_set), write_scan ? scan_set(nxt_set) : ScanPos{nullptr, nullptr},
                        in_slot, (int)it + 1, n, cps, s->status);
-        if (it + 1 < iters ? runs_solver : runs_vort)
+        if (it + 1 < iters && lam_direct)
             k_run_flags<<<grid_for(n + 1), kBlock, 0, st>>>(nxt, n, s->runs);
         mark(5 + 2 * it);
         cur = nxt;
@@ -545,10 +555,14 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
     float4* OM = rec ? rec->OM : s->OM;
     float4* Q = rec ? rec->Q : s->Q;
     launch_commit(g, st, cur, s->perm, s->x, VS, vort ? nullptr : s->v, n, cps);
+    if (va_direct)
+        k_run_flags_vals<<<grid_for(n + 1), kBlock, 0, st>>>(cur, VS, 0, n, s->runs);
     mark(4 + 2 * iters);
     if (vort)
         launch_vorticity_a(s_va, st, cur, s->XP, VS, s->skeys, s->cstart, s->cend, s->VX, OM, Q, nl,
                            pl, scan_set(cur_set), fin_slot, n, cps);
+    if (vb_direct)
+        k_run_flags_vals<<<grid_for(n + 1), kBlock, 0, st>>>(Q, nullptr, 1, n, s->runs);
     mark(5 + 2 * iters);
     if (vort)
         launch_vorticity_b(s_vb, st, Q, s->XP, s->VX, OM, s->skeys, s->perm, s->cstart, s->cend, s->v,

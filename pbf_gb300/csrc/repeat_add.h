@@ -104,4 +104,18 @@ PBF_HD float repeat_add(float r, float w, uint32_t m) {
     return repeat_step(r, m, [w](float x) { return ra_add(x, w); });
 }
 
+#if defined(__CUDACC__)
+// acc <- fma(s, a, acc) per component, m times (fma3 of common.cuh repeated).
+__device__ __forceinline__ float3 repeat_fma3(float s, float3 a, float3 acc, uint32_t m) {
+    return make_float3(repeat_step(acc.x, m, [s, a](float x) { return __fmaf_rn(s, a.x, x); }),
+                       repeat_step(acc.y, m, [s, a](float x) { return __fmaf_rn(s, a.y, x); }),
+                       repeat_step(acc.z, m, [s, a](float x) { return __fmaf_rn(s, a.z, x); }));
+}
+// acc <- acc + a per component, m times (add3 of common.cuh repeated).
+__device__ __forceinline__ float3 repeat_add3(float3 a, float3 acc, uint32_t m) {
+    return make_float3(repeat_add(acc.x, a.x, m), repeat_add(acc.y, a.y, m),
+                       repeat_add(acc.z, a.z, m));
+}
+#endif
+
 }  // namespace pbf

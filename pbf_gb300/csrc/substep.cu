@@ -97,6 +97,35 @@ k_run_flags(const float4* __restrict__ P, uint32_t n, uint32_t* __restrict__ run
     store_run_bits(j, n, p, q, runs);
 }
 
+// Run-start bits over a sweep's whole per-particle input, for the direct
+// sweeps' value runs: particle j starts a run when its position (A.xyz), or
+// A.w (lambda or |vorticity|, with use_w), or B.xyz (the committed velocity,
+// when B is given) differs bitwise from particle j - 1's, or at the stride
+// and terminator marks of store_run_bits.  Inside such a run every candidate
+// gives the same term, so a sweep adds it with repeat_step instead of a loop.
+// Launch over n + 1 threads in whole warps.
+__global__ void __launch_bounds__(kBlock)
+k_run_flags_vals(const float4* __restrict__ A, const float4* __restrict__ B, int use_w,
+                 uint32_t n, uint32_t* __restrict__ runs) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    bool start = j == 0u || j >= n || j % kRunStride == 0u;
+    if (!start) {
+        const float4 a = __ldg(A + j), a0 = __ldg(A + j - 1);
+        start = __float_as_uint(a.x) != __float_as_uint(a0.x) ||
+                __float_as_uint(a.y) != __float_as_uint(a0.y) ||
+                __float_as_uint(a.z) != __float_as_uint(a0.z) ||
+                (use_w && __float_as_uint(a.w) != __float_as_uint(a0.w));
+        if (!start && B) {
+            const float4 b = __ldg(B + j), b0 = __ldg(B + j - 1);
+            start = __float_as_uint(b.x) != __float_as_uint(b0.x) ||
+                    __float_as_uint(b.y) != __float_as_uint(b0.y) ||
+                    __float_as_uint(b.z) != __float_as_uint(b0.z);
+        }
+    }
+    const uint32_t word = __ballot_sync(0xFFFFFFFFu, start);
+    if ((threadIdx.x & 31u) == 0u && (j >> 5) <= (n >> 5)) runs[j >> 5] = word;
+}
+
 // findcells.glsl:34-53 (start of cell(x_0) = 0 and end of cell(x_{n-1}) = n)
 // fused with the gather of the predicted positions into sorted order.
 // Keys >= ncells are skipped and reported through `status` (bad input only).
@@ -450,6 +479,12 @@ k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
     const float3 pi = xyz(P[i]);
     auto ctr = [&] { return stencil_centre(XP[i], c); };  // neighbourcells.glsl:57
     LambdaAcc a{0.0f, 0.0f, make_float3(0.0f, 0.0f, 0.0f)};
+    // in_range: the candidate is known to pass the in-range test (the
+    // masked scans computed the same r2 bit for bit), so the test is skipped
+    auto eval_in = [&](uint32_t j) {
+        const float3 d = sub3(pi, xyz(__ldg(P + j)));
+        lambda_pair(c, d, dot3(d, d), a);
+    };
     auto eval = [&](uint32_t j) {
         const float3 d = sub3(pi, xyz(__ldg(P + j)));
         const float r2 = dot3(d, d);
@@ -477,8 +512,10 @@ k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
     if (!listed) {
         if constexpr (MODE == kPairs)
             scan_then_eval<false>(i, ctr, c, cstart, cend, sx, pi, pw, [](int32_t, uint32_t) {},
-                                  eval);
-        else if (MODE == kDirect && !LISTS && pw.runs)
+                                  eval_in);
+        else if constexpr (MODE == kMasked)
+            sweep_visit<true>(i, ctr, c, cstart, cend, sx, pi, eval_in);
+        else if (!LISTS && pw.runs)
             visit_direct_piles(
                 i, ctr, c, cstart, cend, pw.runs,
                 [&](uint32_t j) { return xyz(__ldg(P + j)); }, pi, eval,
@@ -487,7 +524,7 @@ k_lambda(const float4* __restrict__ P, const float4* __restrict__ XP,
                     lambda_pair_run(c, d, r2, r - j0, a);
                 });
         else
-            sweep_visit<MODE == kMasked>(i, ctr, c, cstart, cend, sx, pi, eval);
+            sweep_visit<false>(i, ctr, c, cstart, cend, sx, pi, eval);
     }
     L[i] = make_float4(pi.x, pi.y, pi.z, lambda_finish(c, a));
     if (aux) aux[i] = lambda_aux(a);
@@ -545,7 +582,8 @@ k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
                         i, ctr, c, cstart, cend, pr.runs,
                         [&](uint32_t j) { return xyz(__ldg(L + j)); }, pi, body, [](uint32_t, uint32_t, uint32_t) {},
                         [&](uint32_t j0, uint32_t r, float3 d, float r2) {
-                            // the same offset for the run: only lambda_j differs
+                            // one offset and, the run bits being over (p, lambda),
+                            // one lambda_j: r - j0 equal terms in a row
                             if (r2 > c.r2cut) return;
                             const float len = fsqrt(r2);
                             float sc = fmul(c.scale, w_poly6(c, len));  // :57
@@ -553,8 +591,8 @@ k_delta_p(const float4* __restrict__ L, const float4* __restrict__ XP,
                             sc = fmul(sc, sc);                           // :59
                             sc = fmul(c.negk, sc);                       // :60
                             const float3 g = scale3(d, grad_scale(c.kg, c.h, len));
-                            for (uint32_t j = j0; j < r; ++j)
-                                dp = fma3(fadd(fadd(li, __ldg(&L[j].w)), sc), g, dp);  // :65
+                            const float coef = fadd(fadd(li, __ldg(&L[j0].w)), sc);  // :65
+                            dp = repeat_fma3(coef, g, dp, r - j0);
                         });
                 else
                     sweep_visit<MODE != kDirect>(i, ctr, c, cstart, cend, sx, pi, body);
@@ -889,10 +927,12 @@ k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
     const float3 vi = xyz(VS[i]);
     auto ctr = [&] { return stencil_centre(XP[i], c); };  // neighbourcells.glsl:57
     float3 acc = make_float3(0.0f, 0.0f, 0.0f), w = make_float3(0.0f, 0.0f, 0.0f);
-    auto eval = [&](uint32_t j) {
+    // body of one candidate; IN: already known to pass the in-range test (the
+    // masked scans computed the same r2 bit for bit)
+    auto body = [&](uint32_t j, auto in) {
         const float3 d = sub3(pi, xyz(__ldg(P + j)));  // :51
         const float r2 = dot3(d, d);
-        if (r2 > c.r2cut) return;
+        if (!decltype(in)::value && r2 > c.r2cut) return;
         const float len = fsqrt(r2);
         const float3 vij = sub3(xyz(__ldg(VS + j)), vi);  // :50
         acc = fma3(w_poly6(c, len), vij, acc);            // :52-54
@@ -900,6 +940,8 @@ k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
         const float3 g = scale3(d, grad_scale(c.kg, c.h, len));
         w = add3(w, cross3(vij, g));  // :55
     };
+    auto eval = [&](uint32_t j) { body(j, std::false_type{}); };
+    auto eval_in = [&](uint32_t j) { body(j, std::true_type{}); };
     bool listed = false;
     if constexpr (LISTS) {
         const int32_t cnt = nl.cnt[i];
@@ -921,29 +963,28 @@ k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
     if (!listed) {
         if constexpr (MODE == kPairs)
             scan_then_eval<false>(i, ctr, c, cstart, cend, sx, pi, pw, [](int32_t, uint32_t) {},
-                                  eval);
-        else if (MODE == kDirect && !LISTS && pw.runs)
+                                  eval_in);
+        else if constexpr (MODE == kMasked)
+            sweep_visit<true>(i, ctr, c, cstart, cend, sx, pi, eval_in);
+        else if (!LISTS && pw.runs)
             visit_direct_piles(
                 i, ctr, c, cstart, cend, pw.runs,
                 [&](uint32_t j) { return xyz(__ldg(P + j)); }, pi, eval,
-                [&](uint32_t j0, uint32_t r, uint32_t) {  // len 0: W(0) (v_j - v_i), no curl
-                    const float w0 = w_poly6(c, 0.0f);
-                    for (uint32_t j = j0; j < r; ++j)
-                        if (j != i) acc = fma3(w0, sub3(xyz(__ldg(VS + j)), vi), acc);
+                // the run bits are over (p, committed v): a run holds one
+                // position and one velocity, so its terms are all equal
+                [&](uint32_t j0, uint32_t, uint32_t m) {  // len 0: W(0) (v_j - v_i), no curl
+                    acc = repeat_fma3(w_poly6(c, 0.0f), sub3(xyz(__ldg(VS + j0)), vi), acc, m);
                 },
-                [&](uint32_t j0, uint32_t r, float3 d, float r2) {  // one offset: v_j differs
+                [&](uint32_t j0, uint32_t r, float3 d, float r2) {
                     if (r2 > c.r2cut) return;
                     const float len = fsqrt(r2);
-                    const float wl = w_poly6(c, len);
                     const float3 g = scale3(d, grad_scale(c.kg, c.h, len));
-                    for (uint32_t j = j0; j < r; ++j) {
-                        const float3 vij = sub3(xyz(__ldg(VS + j)), vi);  // :50
-                        acc = fma3(wl, vij, acc);                         // :52-54
-                        w = add3(w, cross3(vij, g));                      // :55
-                    }
+                    const float3 vij = sub3(xyz(__ldg(VS + j0)), vi);  // :50
+                    acc = repeat_fma3(w_poly6(c, len), vij, acc, r - j0);  // :52-54
+                    w = repeat_add3(cross3(vij, g), w, r - j0);            // :55
                 });
         else
-            sweep_visit<MODE == kMasked>(i, ctr, c, cstart, cend, sx, pi, eval);
+            sweep_visit<false>(i, ctr, c, cstart, cend, sx, pi, eval);
     }
     const float3 vx = fma3(c.cx, acc, vi);  // :58
     VX[i] = make_float4(vx.x, vx.y, vx.z, 0.0f);
@@ -993,11 +1034,11 @@ k_vorticity_b(const float4* __restrict__ Q, const float4* __restrict__ XP,
                     i, ctr, c, cstart, cend, pr.runs,
                     [&](uint32_t j) { return xyz(__ldg(Q + j)); }, pi, body, [](uint32_t, uint32_t, uint32_t) {},
                     [&](uint32_t j0, uint32_t r, float3 d, float r2) {
-                        // the same offset for the run: only |omega_j| differs
+                        // one offset and, the run bits being over (p, |omega|),
+                        // one |omega_j|: r - j0 equal terms in a row
                         if (r2 > c.r2cut) return;
                         const float3 g = scale3(d, grad_scale(c.kg, c.h, fsqrt(r2)));
-                        for (uint32_t j = j0; j < r; ++j)
-                            eta = fma3(__ldg(&Q[j].w), g, eta);  // :72
+                        eta = repeat_fma3(__ldg(&Q[j0].w), g, eta, r - j0);  // :72
                     });
             else
                 sweep_visit<MODE != kDirect>(i, ctr, c, cstart, cend, sx, pi, body);
@@ -1271,6 +1312,7 @@ cudaError_t preload_sweeps() {
     load((const void*)k_vorticity_a_coop<CP>);
     load((const void*)k_vorticity_b_coop<CP>);
     load((const void*)k_run_flags);
+    load((const void*)k_run_flags_vals);
     return e;
 }
 template cudaError_t preload_sweeps<OneScene>();

@@ -9,6 +9,8 @@ namespace pbf {
 __global__ void k_unmark_cells(const uint32_t* __restrict__ prev_sorted, uint32_t n,
                                uint32_t ncells, int32_t* __restrict__ cstart);
 __global__ void k_run_flags(const float4* __restrict__ P, uint32_t n, uint32_t* __restrict__ runs);
+__global__ void k_run_flags_vals(const float4* __restrict__ A, const float4* __restrict__ B,
+                                 int use_w, uint32_t n, uint32_t* __restrict__ runs);
 __global__ void k_find_cells(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
                              const float4* __restrict__ xstar, float4* __restrict__ P0, uint32_t n,
                              uint32_t ncells, int32_t* __restrict__ cstart,
