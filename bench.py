@@ -65,6 +65,14 @@ def parse():
     ap.add_argument("--no-full", action="store_true",
                     help="skip the full 500-substep run of the workload itself")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-scene comparison")
+    ap.add_argument("--plain-every", type=int, default=8,
+                    help="step every k-th of the 256 scenes plainly for the comparison (1: all)")
+    ap.add_argument("--full-budget", type=float, default=90.0,
+                    help="seconds of the workload's own 500-substep run; it stops after the "
+                         "25-substep segment that crosses the budget (0: run all 500)")
+    ap.add_argument("--recovery-steps-eps001", type=int, default=5,
+                    help="gradient-descent steps of the recovery at the workload's epsilon "
+                         "(its gradients are not finite; 50 at epsilon = 5)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the backward/forward ratio")
     ap.add_argument("--no-splat", action="store_true", help="skip the depth/thickness splatting leg")
     ap.add_argument("--no-small", action="store_true", help="skip the 16,384-particle configuration")
@@ -160,12 +168,16 @@ def profiled_traffic():
         return None
 
 
-def batched_vs_plain(stream, num_scenes: int = 256, substeps: int = 100):
+def batched_vs_plain(stream, num_scenes: int = 256, substeps: int = 100, plain_every: int = 8):
     """256 dam breaks (4,096-65,536 particles, boxes 32-96 cells, 4 iterations,
     100 substeps): one batched handle (every stage one launch over all scenes,
-    the substep replayed as one CUDA graph) against the same scenes stepped
-    one at a time, each in its own handle with its own graph, on the same
-    stream.  Both start from the initial scenes after 3 warm-up substeps."""
+    the substep replayed as one CUDA graph) against the scenes stepped one at a
+    time, each in its own handle with its own graph, on the same stream.  Both
+    start from the initial scenes after 3 warm-up substeps.  With epsilon =
+    0.01 the scenes collapse and stepping all 256 plainly takes ~10 minutes,
+    so by default every `plain_every`-th scene (32 of 256) is stepped plainly
+    and the plain time of all 256 is that sample's time x 256 / 32
+    (plain_every = 1: all of them)."""
     import torch
     import numpy as np
     import pbf_gb300 as pg
@@ -177,8 +189,10 @@ def batched_vs_plain(stream, num_scenes: int = 256, substeps: int = 100):
     batch.set_state(x4, v4)
     batch.step(3)
     batch.set_state(x4, v4)
+    sample = list(range(0, num_scenes, plain_every))
     plain = []
-    for s in scs:
+    for k in sample:
+        s = scs[k]
         h = pg.SPH(s.n, tuple(s.params.grid), s.params)
         h.set_stream(stream.cuda_stream)
         h.set_state(s.x4, s.v4)
@@ -197,11 +211,12 @@ def batched_vs_plain(stream, num_scenes: int = 256, substeps: int = 100):
     e[3].record(stream)
     torch.cuda.synchronize()
     tb = e[0].elapsed_time(e[1])
-    tp = e[2].elapsed_time(e[3])
+    tps = e[2].elapsed_time(e[3])
+    tp = tps * num_scenes / len(sample)
     bx, bv = batch.get_state()
     same = True
-    for k in range(0, num_scenes, max(1, num_scenes // 16)):
-        px, pv = plain[k].get_state()
+    for h, k in zip(plain, sample):
+        px, pv = h.get_state()
         sl = batch.scene_slice(k)
         same = same and np.array_equal(bx[sl].view(np.uint32), px.view(np.uint32)) and \
             np.array_equal(bv[sl].view(np.uint32), pv.view(np.uint32))
@@ -211,11 +226,15 @@ def batched_vs_plain(stream, num_scenes: int = 256, substeps: int = 100):
         h.close()
     batch.close()
     return {"scenes": num_scenes, "particles": n, "substeps": substeps,
-            "batched_ms": tb, "plain_ms": tp,
+            "batched_ms": tb, "plain_ms": tp, "plain_sampled_scenes": len(sample),
+            "plain_sampled_ms": tps,
             "batched_scenes_per_s": num_scenes / (tb * 1e-3),
             "plain_scenes_per_s": num_scenes / (tp * 1e-3), "speedup": tp / tb,
             "batched_particle_iters_per_s": n * it * substeps / (tb * 1e-3),
-            "bit_identical_sampled_scenes": bool(same)}
+            "bit_identical_sampled_scenes": bool(same),
+            "note": ("plain time of all 256 scenes estimated from every "
+                     f"{plain_every}th scene stepped plainly" if plain_every > 1 else
+                     "every scene stepped plainly")}
 
 
 def batched_sharded(stream, rank: int, world: int, barrier, num_scenes: int = 256,
@@ -580,8 +599,11 @@ def legs_summary(stable, full, batched, adjoint, adjoint5, small, recov, sharded
         out["batched_256_sharded"] = _sig({"ranks": sharded["ranks"],
                                            "scenes_per_s": sharded["scenes_per_s"]})
     if full:
-        out["full_500"] = _sig({"value": full["value"], "ms_per_step": full["ms_per_step"],
-                                "ms_per_step_by_100": full["ms_per_step_by_100"]})
+        by = full["ms_per_step_by_25"]
+        out["full_500"] = _sig({"value": full["value"], "substeps": full["substeps"],
+                                "ms_per_step": full["ms_per_step"],
+                                "ms_per_step_by_100": [sum(by[k:k + 4]) / len(by[k:k + 4])
+                                                       for k in range(0, len(by), 4)]})
     if stable:
         out["stable_500_eps5"] = _sig({"value": stable["value"], "ms_per_step": stable["ms_per_step"]})
     if small:
@@ -633,6 +655,13 @@ def main():
     def barrier():
         if world > 1:
             dist.barrier()
+
+    t_leg = [time.perf_counter()]
+
+    def leg_done(name):  # progress on stderr: wall seconds of each leg
+        now = time.perf_counter()
+        print(f"bench: {name} {now - t_leg[0]:.1f} s", file=sys.stderr, flush=True)
+        t_leg[0] = now
 
     K, W = args.steps, max(3, args.warmup)
     it = scene.params.num_solver_iterations
@@ -726,6 +755,7 @@ def main():
 
     # the same scene with the reference's default epsilon: a stable run of
     # the full 500 substeps
+    leg_done('window, e2e and stage timing')
     stable = None
     if not args.no_stable:
         ps = scene.params.copy()
@@ -757,59 +787,78 @@ def main():
     # the workload's own full run (epsilon = 0.01, all substeps): the fluid
     # collapses into dense clumps and corner piles after ~100 substeps, where
     # the automatic sweep configuration moves to the direct sweeps
+    leg_done('stable_500')
     full = None
     if not args.no_full:
+        # 25-substep segments, host-synchronised, until the budget is spent
         sim.set_state(scene.x4, scene.v4)
         torch.cuda.synchronize()
-        seg = 100
-        fev = [torch.cuda.Event(enable_timing=True) for _ in range(scene.substeps // seg + 1)]
-        fev[0].record(stream)
-        for k in range(scene.substeps // seg):
+        seg = 25
+        seg_ms = []
+        t_start = time.perf_counter()
+        while len(seg_ms) * seg < scene.substeps:
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
             sim.step(seg)
-            fev[k + 1].record(stream)
-        torch.cuda.synchronize()
+            b.record(stream)
+            b.synchronize()
+            seg_ms.append(a.elapsed_time(b))
+            if args.full_budget > 0 and time.perf_counter() - t_start > args.full_budget:
+                break
         sim.synchronize()
-        fms = fev[0].elapsed_time(fev[-1])
-        full = {"value": scene.n * it * scene.substeps / (fms * 1e-3), "unit": UNIT,
-                "substeps": scene.substeps, "ms_per_step": fms / scene.substeps,
-                "ms_per_step_by_100": [fev[k].elapsed_time(fev[k + 1]) / seg
-                                       for k in range(len(fev) - 1)],
+        done = len(seg_ms) * seg
+        fms = sum(seg_ms)
+        full = {"value": scene.n * it * done / (fms * 1e-3), "unit": UNIT,
+                "substeps": done, "of_substeps": scene.substeps, "ms_per_step": fms / done,
+                "ms_per_step_by_25": seg_ms and [t / seg for t in seg_ms],
+                "complete": done == scene.substeps,
                 "sweep_choice_after": sim.sweep_choice(),
                 "state_after": sim.diagnostics(),
-                "note": "graph replay with the default automatic sweep configuration "
-                        "(its trials are real substeps of the run)"}
+                "note": "graph replay with the default automatic sweep configuration (its "
+                        "trials are real substeps of the run); "
+                        + ("all substeps" if done == scene.substeps else
+                           f"stopped after {done} substeps at the --full-budget of "
+                           f"{args.full_budget:.0f} s")}
 
+    leg_done('full_500')
     adjoint = adjoint5 = None
     if not args.no_adjoint:
         adjoint = adjoint_ratio(stream)
         adjoint5 = adjoint_ratio(stream, epsilon=5.0)
+    leg_done('adjoint')
     splats = None
     if not args.no_splat:
         splats = splat_leg(stream)
 
+    leg_done('splat')
     recov = None
     if not args.no_recovery:
-        recov = {"workload_epsilon_0.01": recovery(stream),
+        recov = {"workload_epsilon_0.01": recovery(stream, steps=args.recovery_steps_eps001),
                  "reference_default_epsilon_5": recovery(stream, epsilon=5.0)}
 
+    leg_done('recovery')
     batched = None
     if not args.no_batched:
         sim.close()
         torch.cuda.empty_cache()
-        batched = batched_vs_plain(stream)
+        batched = batched_vs_plain(stream, plain_every=args.plain_every)
+    leg_done('batched_256')
     sharded = None
     if world > 1:
         sim.close()
         torch.cuda.empty_cache()
         sharded = batched_sharded(stream, rank, world, barrier)
 
+    leg_done('sharded batch')
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args.scene, args.cpu_substeps)
+    leg_done('cpu baseline')
     small = None
     if not args.no_small:
         small = small_config(stream, rank == 0 and world == 1 and not args.no_cpu_baseline)
 
+    leg_done('dam_break_16k_200')
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,

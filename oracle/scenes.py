@@ -143,6 +143,11 @@ def plain_2m(seed: int = 0) -> Scene:
     return dam_break((128, 128, 128), (256, 128, 256), 4, 500, seed, "dam_break_2m")
 
 
+def plain_262k(seed: int = 0) -> Scene:
+    """262,144 particles (64^3) in a 128x64x128 box, 4 iterations."""
+    return dam_break((64, 64, 64), (128, 64, 128), 4, 500, seed, "dam_break_262k")
+
+
 def diff_32k(seed_a: int = 1, seed_b: int = 2):
     """32,768 particles (32^3) in a 64^3 box, velocities N(0, 0.25^2) from
     seed A and seed B, 64 substeps x 4 iterations."""

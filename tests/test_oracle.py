@@ -235,7 +235,7 @@ def test_oracle_scenes_equal_the_product_generator(oracle_mod, product_lib):
     from oracle import scenes as oscenes
     assert C.sizeof(oscenes.Params) == C.sizeof(Params)
     assert [f for f, _ in oscenes.Params._fields_] == [f for f, _ in Params._fields_]
-    for name in ("plain_16k", "plain_2m"):
+    for name in ("plain_16k", "plain_262k", "plain_2m"):
         a, b = getattr(oscenes, name)(), getattr(scenes, name)()
         assert a.name == b.name and a.substeps == b.substeps and a.meta == b.meta
         assert bytes(a.params) == bytes(b.params), name
