@@ -237,15 +237,18 @@ typedef struct pbf_tuning {
  * events, and the handle keeps the fastest solver and vorticity
  * configurations.  Every configuration gives the same bits, so trials change
  * no result; skin lists are not used.  Handles start with PBF_PASS_COOP below
- * 32,768 particles and PBF_PASS_MASKED from there. */
+ * 32,768 particles and PBF_PASS_MIXED from there (a thread per particle, and
+ * a warp for each particle in a dense stencil). */
 enum { PBF_SWEEP_DIRECT = 0, PBF_SWEEP_MASKED = 1, PBF_SWEEP_COOP = 2, PBF_SWEEP_AUTO = 3 };
 enum {
     PBF_PASS_MASKED = 0,      /* masked scans (with pair lists when pair_list_capacity > 0) */
     PBF_PASS_DIRECT = 1,      /* direct stencil loops */
     PBF_PASS_COOP = 2,        /* warp-cooperative sweeps */
-    PBF_PASS_DIRECT_COOP = 3  /* direct first sweep (lambda, vorticity a), cooperative second
+    PBF_PASS_DIRECT_COOP = 3, /* direct first sweep (lambda, vorticity a), cooperative second
                                  (delta-p, vorticity b); not among the automatic mode's
                                  candidates (its cooperative sweeps walk piles pair by pair) */
+    PBF_PASS_MIXED = 4        /* masked scans, and warp-cooperative sweeps for the particles
+                                 with more than coop_candidates (0: 256) stencil candidates */
 };
 
 /* No reference counterpart (the reference has no tuning surface). */

@@ -36,6 +36,7 @@ PBF_PASS_MASKED = 0
 PBF_PASS_DIRECT = 1
 PBF_PASS_COOP = 2
 PBF_PASS_DIRECT_COOP = 3
+PBF_PASS_MIXED = 4
 
 
 class Params(C.Structure):

@@ -177,7 +177,7 @@ void reset_sweep_choice(pbf_sim* s) {
     uint32_t pass = m == PBF_SWEEP_DIRECT ? PBF_PASS_DIRECT
                     : m == PBF_SWEEP_COOP ? PBF_PASS_COOP
                                           : PBF_PASS_MASKED;
-    if (m == PBF_SWEEP_AUTO) pass = s->n < kCoopBelow ? PBF_PASS_COOP : PBF_PASS_MASKED;
+    if (m == PBF_SWEEP_AUTO) pass = s->n < kCoopBelow ? PBF_PASS_COOP : PBF_PASS_MIXED;
     s->pass_solver = s->pass_vort = pass;
     s->autop.reset(s->tuning.auto_period);
     s->auto_trial = -1;
@@ -188,7 +188,8 @@ void reset_sweep_choice(pbf_sim* s) {
 // small and then costs O(pile^2 / 32) as they grow, where the direct sweeps
 // stay fast.)
 void pick_trial_candidates(pbf_sim* s) {
-    s->auto_cands = s->autop.candidates(s->pass_solver, s->pass_vort, s->n < kCoopTrialBelow);
+    s->auto_cands = s->autop.candidates(s->pass_solver, s->pass_vort, s->n < kCoopTrialBelow,
+                                        s->n >= kCoopBelow);
 }
 
 // SweepCfg modes (0 direct, 1 masked, 2 masked + pair lists, 3 cooperative)
@@ -210,12 +211,22 @@ PassModes modes_of(const pbf_sim* s, uint32_t pass) {
 bool skin_lists_on(const pbf_sim* s) {
     return s->tuning.use_neighbour_lists != 0 && s->tuning.sweep_mode != PBF_SWEEP_AUTO;
 }
-// Mixed sweeps run when asked for and some sweep runs a thread per particle.
+// Whether a pass's one-thread sweeps leave the heavy particles to warps:
+// every such pass when coop_candidates is set (the opt-in mixed sweeps), and
+// the PBF_PASS_MIXED configuration (threshold coop_candidates, or 256).
+bool pass_mixed(const pbf_sim* s, uint32_t pass) {
+    if (skin_lists_on(s)) return false;
+    if (pass == PBF_PASS_MIXED) return true;
+    if (s->tuning.coop_candidates == 0) return false;
+    const PassModes m = modes_of(s, pass);
+    return m.first != 3 || m.second != 3;
+}
 bool mixed_on(const pbf_sim* s) {
-    if (s->tuning.coop_candidates == 0 || skin_lists_on(s)) return false;
-    const PassModes a = modes_of(s, s->pass_solver), b = modes_of(s, s->pass_vort);
     const bool vort = s->params.vorticity_confinement != 0;
-    return a.first != 3 || a.second != 3 || (vort && (b.first != 3 || b.second != 3));
+    return pass_mixed(s, s->pass_solver) || (vort && pass_mixed(s, s->pass_vort));
+}
+uint32_t heavy_threshold(const pbf_sim* s) {
+    return s->tuning.coop_candidates ? s->tuning.coop_candidates : kMixedCandidates;
 }
 
 // Host-side fault injection (pbf_debug_fail_allocation): when armed, the
@@ -286,7 +297,7 @@ void free_sim(pbf_sim* s) {
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
     free_tape(s);
-    for (int k = 0; k < 16; ++k) {
+    for (int k = 0; k < 25; ++k) {
         if (s->execs[k]) cudaGraphExecDestroy(s->execs[k]);
         if (s->graphs[k]) cudaGraphDestroy(s->graphs[k]);
     }
@@ -328,8 +339,9 @@ uint32_t kernels_per_substep(const pbf_sim* s) {
     }
     if (mixed_on(s)) {  // the flag pass and a cooperative launch after each one-thread sweep
         const PassModes a = modes_of(s, s->pass_solver), b = modes_of(s, s->pass_vort);
-        k += 1u + iters * ((a.first != 3) + (a.second != 3)) +
-             (vort ? (uint32_t)((b.first != 3) + (b.second != 3)) : 0u);
+        k += 1u;
+        if (pass_mixed(s, s->pass_solver)) k += iters * ((a.first != 3) + (a.second != 3));
+        if (vort && pass_mixed(s, s->pass_vort)) k += (uint32_t)((b.first != 3) + (b.second != 3));
     }
     return k;
 }
@@ -341,7 +353,7 @@ pbf_status timed_substep(pbf_sim* s);
 // Launches `count` substeps of the captured graph of the current solver and
 // vorticity configurations (captured on first use).
 pbf_status launch_graph(pbf_sim* s, uint32_t count) {
-    const uint32_t key = s->pass_solver * 4u + s->pass_vort;
+    const uint32_t key = s->pass_solver * 5u + s->pass_vort;
     if (!s->execs[key]) {
         PBF_CUDA(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
         cudaError_t e = enqueue_substep(s, nullptr);
@@ -492,7 +504,7 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
     if (mixed) {
         cudaError_t me = cudaMemsetAsync(s->heavy_count, 0, sizeof(uint32_t), st);
         if (me != cudaSuccess) return me;
-        launch_heavy_scan(g, st, s->XP, s->cstart, s->cend, s->tuning.coop_candidates, n, cps,
+        launch_heavy_scan(g, st, s->XP, s->cstart, s->cend, heavy_threshold(s), n, cps,
                           s->heavy, s->heavy_list, s->heavy_count);
     }
     mark(3);
@@ -509,9 +521,14 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
     const bool vb_direct = !lists && vort && mv.second == 0;
     const bool runs_solver = lam_direct || dp_direct;
     const bool runs_vort = va_direct || vb_direct;
-    const PairLists pl{s->pair_idx, s->pair_cnt, s->pair_cap, n, mixed ? s->heavy : nullptr,
+    // the heavy list goes only to the passes that leave heavy particles to warps
+    const bool mix_s = mixed && pass_mixed(s, s->pass_solver);
+    const bool mix_v = mixed && pass_mixed(s, s->pass_vort);
+    const PairLists pl{s->pair_idx, s->pair_cnt, s->pair_cap, n, mix_s ? s->heavy : nullptr,
                        s->heavy_list, s->heavy_count,
                        runs_solver || runs_vort ? s->runs : nullptr};
+    PairLists pl_v = pl;
+    pl_v.heavy = mix_v ? s->heavy : nullptr;
     cudaError_t ge = cudaMemsetAsync(s->guard, 0, sizeof(uint32_t) * (2 + iters), st);
     if (ge != cudaSuccess) return ge;
     const float4* cur = s->XP;
@@ -560,13 +577,13 @@ cudaError_t enqueue_impl(pbf_sim* s, cudaEvent_t* ev, const Recording* rec, cons
     mark(4 + 2 * iters);
     if (vort)
         launch_vorticity_a(s_va, st, cur, s->XP, VS, s->skeys, s->cstart, s->cend, s->VX, OM, Q, nl,
-                           pl, scan_set(cur_set), fin_slot, n, cps);
+                           pl_v, scan_set(cur_set), fin_slot, n, cps);
     if (vb_direct)
         k_run_flags_vals<<<grid_for(n + 1), kBlock, 0, st>>>(Q, nullptr, 1, n, s->runs);
     mark(5 + 2 * iters);
     if (vort)
         launch_vorticity_b(s_vb, st, Q, s->XP, s->VX, OM, s->skeys, s->perm, s->cstart, s->cend, s->v,
-                           rec ? rec->ETA : nullptr, nl, pl, scan_set(cur_set), fin_slot, n, cps);
+                           rec ? rec->ETA : nullptr, nl, pl_v, scan_set(cur_set), fin_slot, n, cps);
     mark(6 + 2 * iters);
     return cudaGetLastError();
 }
@@ -578,7 +595,7 @@ cudaError_t enqueue_substep(pbf_sim* s, cudaEvent_t* ev, const Recording* rec) {
 }
 
 void invalidate_graph(pbf_sim* s) {
-    for (int k = 0; k < 16; ++k) {
+    for (int k = 0; k < 25; ++k) {
         if (s->execs[k]) cudaGraphExecDestroy(s->execs[k]);
         if (s->graphs[k]) cudaGraphDestroy(s->graphs[k]);
         s->execs[k] = nullptr;

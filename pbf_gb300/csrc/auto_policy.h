@@ -7,7 +7,8 @@
 //  - the first trial comes `base` substeps after a reset (state upload,
 //    tuning change);
 //  - a trial steps one substep under each candidate: masked and direct, and
-//    cooperative where the scene is small enough (the caller decides);
+//    mixed and cooperative where the scene size suits them (the caller
+//    decides);
 //  - a candidate replaces the current configuration of the solver pass or
 //    the vorticity pass when its time for that pass is below kAutoMargin
 //    times the current one's;
@@ -42,8 +43,8 @@ struct AutoPolicy {
     uint64_t count = 0;            // substeps since the last reset
     uint64_t next = kAutoPeriod;   // substep at which the next trial starts
     double last_ms = 0.0;          // the chosen configurations' time at the last trial
-    uint32_t skip[4] = {};         // trials a configuration still sits out
-    uint32_t skip_len[4] = {};     // its last sit-out
+    uint32_t skip[5] = {};         // trials a configuration still sits out
+    uint32_t skip_len[5] = {};     // its last sit-out
     uint32_t trials = 0;
 
     void reset(uint32_t base_period) {
@@ -59,8 +60,10 @@ struct AutoPolicy {
     bool trial_due() const { return count >= next; }
 
     // The next trial's candidates (PBF_PASS_*), given the current choices.
-    std::vector<uint32_t> candidates(uint32_t solver, uint32_t vort, bool try_coop) {
+    std::vector<uint32_t> candidates(uint32_t solver, uint32_t vort, bool try_coop,
+                                     bool try_mixed = false) {
         std::vector<uint32_t> all = {PBF_PASS_MASKED, PBF_PASS_DIRECT};
+        if (try_mixed) all.push_back(PBF_PASS_MIXED);
         if (try_coop) all.push_back(PBF_PASS_COOP);
         std::vector<uint32_t> out;
         for (uint32_t p : all) {

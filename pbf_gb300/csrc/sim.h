@@ -75,8 +75,8 @@ struct pbf_sim {
     // PBF_PASS_* configuration of the solver sweeps and the vorticity passes
     // the next substep runs; one captured graph per pair
     uint32_t pass_solver = 0, pass_vort = 0;
-    cudaGraph_t graphs[16] = {};
-    cudaGraphExec_t execs[16] = {};
+    cudaGraph_t graphs[25] = {};  // one per (solver pass, vorticity pass): 5 x 5
+    cudaGraphExec_t execs[25] = {};
 
     // PBF_SWEEP_AUTO: the schedule and sit-outs (auto_policy.h), the
     // candidate the running trial steps next (-1: none), the trial's

@@ -196,7 +196,7 @@ class SPH:
             t.auto_period = int(auto_period)
         check(self._lib.pbf_set_tuning(self._h, C.byref(t)), self._h)
 
-    PASSES = ("masked", "direct", "coop", "direct+coop")
+    PASSES = ("masked", "direct", "coop", "direct+coop", "mixed")
 
     def sweep_choice(self) -> dict:
         """The configurations the next substep runs for the solver sweeps and

@@ -38,6 +38,20 @@ int main() {
     CHECK(solver == D && vort == M);
     CHECK(p.period == 32 && p.next == 34 + 1 + 32 && p.trials == 1);
     CHECK(p.skip[C] == 3 && p.skip_len[C] == 3 && p.skip[M] == 0 && p.skip[D] == 0);
+    {   // the mixed configuration joins the candidates where the caller asks for it
+        AutoPolicy q;
+        q.reset(0);
+        const uint32_t X = PBF_PASS_MIXED;
+        CHECK(same(q.candidates(X, X, false, true), {M, D, X}));
+        CHECK(same(q.candidates(X, X, false, false), {M, D, X}));  // the current choice runs
+        CHECK(same(q.candidates(M, M, true, true), {M, D, X, C}));
+        double s[] = {10.0, 9.5, 6.0, 30.0}, v[] = {5.0, 5.0, 4.0, 20.0};
+        uint32_t a = M, b = M;
+        std::vector<uint32_t> cq = q.candidates(a, b, true, true);
+        q.count = 32;
+        q.finish(cq, s, v, true, a, b);
+        CHECK(a == X && b == X && q.skip[C] == 3);
+    }
     // trial 2: coop sits out; a candidate only 2% faster does not switch
     c = p.candidates(solver, vort, true);
     CHECK(same(c, {M, D}) && p.skip[C] == 2);

@@ -292,7 +292,7 @@ def test_auto_sweeps_never_change_results(gpu, oracle_mod, extra):
 
 def test_auto_is_the_default_and_resets(gpu):
     """Handles default to PBF_SWEEP_AUTO, starting with the cooperative
-    sweeps below 32,768 particles and the masked sweeps from there; a state
+    sweeps below 32,768 particles and the mixed sweeps from there; a state
     upload restarts the trial schedule (the first trial after auto_period
     substeps)."""
     sc = scenes.plain_16k()
@@ -311,7 +311,27 @@ def test_auto_is_the_default_and_resets(gpu):
     assert g.sweep_choice() == {"solver": "coop", "vorticity": "coop", "trials": 0}
     big = scenes.dam_break((40, 40, 40), (80, 80, 80), 4, 100, 0, "auto")
     h = pg.SPH(big.n, tuple(big.params.grid), big.params)
-    assert h.sweep_choice()["solver"] == "masked"
+    assert h.sweep_choice()["solver"] == "mixed"
+
+
+def test_auto_sweeps_with_the_mixed_candidate_never_change_results(gpu, oracle_mod):
+    """From 32,768 particles the automatic configuration starts with the
+    mixed sweeps (a warp for each particle with more than 256 stencil
+    candidates) and also tries them in its trials, next to masked, direct and
+    cooperative; every switch keeps the oracle's bits."""
+    sc = scenes.dam_break((40, 40, 40), (80, 80, 80), 4, 100, 0, "auto_mixed")
+    g = pg.SPH(sc.n, tuple(sc.params.grid), sc.params)
+    g.set_tuning(sweep_mode="auto", auto_period=2)
+    g.set_state(sc.x4, sc.v4)
+    assert g.sweep_choice() == {"solver": "mixed", "vorticity": "mixed", "trials": 0}
+    for _ in range(6):
+        g.step(5)
+    assert g.sweep_choice()["trials"] >= 3
+    o = run_oracle(oracle_mod, sc.params, sc.x4, sc.v4, 30)
+    x, v = g.get_state()
+    ox, ov = o.get_state()
+    assert_bits(x, ox, "positions under automatic sweeps with the mixed candidate")
+    assert_bits(v, ov, "velocities under automatic sweeps with the mixed candidate")
 
 
 def test_lists_exact_in_a_calm_scene(gpu, oracle_mod):
