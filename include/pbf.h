@@ -237,8 +237,9 @@ typedef struct pbf_tuning {
  * events, and the handle keeps the fastest solver and vorticity
  * configurations.  Every configuration gives the same bits, so trials change
  * no result; skin lists are not used.  Handles start with PBF_PASS_COOP below
- * 32,768 particles and PBF_PASS_MIXED from there (a thread per particle, and
- * a warp for each particle in a dense stencil). */
+ * 32,768 particles and from there with PBF_PASS_MIXED (a thread per particle,
+ * and a warp for each particle in a dense stencil) for one scene and
+ * PBF_PASS_MASKED for a batch. */
 enum { PBF_SWEEP_DIRECT = 0, PBF_SWEEP_MASKED = 1, PBF_SWEEP_COOP = 2, PBF_SWEEP_AUTO = 3 };
 enum {
     PBF_PASS_MASKED = 0,      /* masked scans (with pair lists when pair_list_capacity > 0) */

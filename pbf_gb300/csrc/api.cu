@@ -177,7 +177,12 @@ void reset_sweep_choice(pbf_sim* s) {
     uint32_t pass = m == PBF_SWEEP_DIRECT ? PBF_PASS_DIRECT
                     : m == PBF_SWEEP_COOP ? PBF_PASS_COOP
                                           : PBF_PASS_MASKED;
-    if (m == PBF_SWEEP_AUTO) pass = s->n < kCoopBelow ? PBF_PASS_COOP : PBF_PASS_MIXED;
+    // (mixed for one large scene: the 2M dam break's window runs 2.1x faster
+    // under it than masked; a batch of small scenes starts masked, where mixed
+    // measured slower)
+    if (m == PBF_SWEEP_AUTO)
+        pass = s->n < kCoopBelow ? PBF_PASS_COOP
+                                 : (s->nscenes == 1 ? PBF_PASS_MIXED : PBF_PASS_MASKED);
     s->pass_solver = s->pass_vort = pass;
     s->autop.reset(s->tuning.auto_period);
     s->auto_trial = -1;
