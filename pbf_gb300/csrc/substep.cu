@@ -366,10 +366,11 @@ __device__ __forceinline__ float lambda_finish(const DevConsts& c, const LambdaA
 // 6 or 4 blocks with more registers measured slower).  One thread per sorted
 // particle.
 constexpr int kSweepBlocksPerSM = 8;
-// The direct first vorticity pass carries the run path's extra state (its
-// velocity loops over coincident and equal-offset runs): 6 blocks per SM
-// (40 registers) keep it from spilling in those loops.
-constexpr int kDirectVortBlocksPerSM = 6;
+// The first vorticity pass carries more state than the other sweeps (the
+// XSPH and vorticity sums, the velocity, the run path's repeated steps): 6
+// blocks per SM (40 registers) keep it from spilling; measured 10% faster
+// than 8 blocks with spills on the 2M window.
+constexpr int kVortBlocksPerSM = 6;
 
 // Instantiations of the sweep kernels (pbf_tuning): MODE is the stencil scan
 // (kDirect: the reference's loop shape; kMasked: masked scans; kPairs: masked
@@ -914,7 +915,7 @@ k_commit(const float4* __restrict__ P, const uint32_t* __restrict__ perm, float4
 // vorticity.glsl:34-60: XSPH velocity and the vorticity vector, Jacobi
 // (every read sees the committed velocities).
 template <class CP, int MODE, bool LISTS>
-__global__ void __launch_bounds__(kBlock, MODE == kDirect ? kDirectVortBlocksPerSM : kSweepBlocksPerSM)
+__global__ void __launch_bounds__(kBlock, kVortBlocksPerSM)
 k_vorticity_a(const float4* __restrict__ P, const float4* __restrict__ XP,
               const float4* __restrict__ VS, const uint32_t* __restrict__ skeys,
               const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
