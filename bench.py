@@ -5,9 +5,10 @@ on the 2,097,152-particle dam break (128^3 lattice, spacing 0.5h, in a
 
 A "step" is one substep (SPH::Run) over all particles.  The timed window is
 substeps 1..K of the run (default K = 50): with the workload's constants
-(epsilon = 0.01, the reference's unclamped density constraint) the dam break
-blows up after about 60 substeps and collapses into clumps of thousands of
-particles per cell, a different and degenerate workload; `stable_500`
+(epsilon = 0.01, the reference's unclamped density constraint and stencil
+centre) the dam break blows up within the first 20 substeps and then
+collapses into clumps of thousands of particles per cell, a different and
+degenerate workload; `stable_500`
 reports the same scene with the reference's default CFM epsilon (5) over
 the full 500 substeps.  Timed regions:
   value    K substeps replayed from the captured CUDA graph, inputs resident
@@ -17,7 +18,9 @@ the full 500 substeps.  Timed regions:
            one substep (pbf_step) and reads the state back (pbf_get_state);
   kernels  the same K substeps replayed eagerly with CUDA events around
            every kernel, for the per-launch durations behind `roofline`.
-Each timed run starts from the initial scene, after W warm-up substeps.
+Each timed run starts from the initial scene, after W warm-up substeps;
+the e2e steps continue one trajectory (each uploads the state the step
+before it read back).
 The per-substep working set (~0.5 GB) is larger than L2, so L2 is not
 flushed between steps.
 

@@ -229,6 +229,11 @@ typedef struct pbf_tuning {
                                      between trials while the choice or its measured
                                      time keeps changing (doubling up to 256 substeps
                                      while both hold); 0 = 32 */
+    uint32_t adjoint_warp_candidates; /* pbf_backward: particles whose stencil holds more
+                                     than this many candidates get a warp each in the
+                                     reverse neighbour sweeps (their pair terms summed
+                                     across its lanes), the others a thread; 0 = 256;
+                                     0xFFFFFFFF: a thread for every particle */
 } pbf_tuning;
 
 /* PBF_SWEEP_AUTO (default): the solver sweeps (lambda + delta-p) and the two

@@ -85,6 +85,7 @@ class Tuning(C.Structure):
         ("pair_list_capacity", C.c_uint32),
         ("coop_candidates", C.c_uint32),
         ("auto_period", C.c_uint32),
+        ("adjoint_warp_candidates", C.c_uint32),
     ]
 
 

@@ -72,7 +72,10 @@ struct Tape {
     float4 *XSB = nullptr, *XOB = nullptr;  // x*-bar and x_old-bar (id order)
     double* acc = nullptr;                  // [kParams][n] per-particle parameter gradients (id order)
     uint8_t* irr = nullptr;                 // [n] stencil centre != key cell (sorted), per substep
-    uint32_t* any_irr = nullptr;            // whether any particle of the substep is so
+    uint32_t* words = nullptr;              // [2]: any particle irregular; flagged particles
+    uint8_t* heavy = nullptr;               // [n] swept by a warp (sorted), per substep
+    uint32_t* heavy_list = nullptr;         // [n] those particles
+    uint32_t warp_above = 0;                // candidates above which a particle gets a warp
     std::vector<void*> owned;
 };
 
@@ -255,6 +258,56 @@ __device__ __forceinline__ void adj_visit_again(uint32_t i, Ctr&& ctr, const Dev
         visit_full(i, ctr, c, cstart, cend, f);
 }
 
+// ---- a warp per particle for dense stencils ---------------------------------------
+//
+// A thread per particle leaves a dense stencil to one thread's serial loop
+// over thousands of candidates (collapsed states: the 32,768-particle
+// epsilon = 0.01 run holds piles of up to ~11,000 particles by substep 40),
+// and with few particles per SM the slowest such thread sets the launch time.
+// Particles whose key-cell stencil holds more than `warp_above` candidates
+// are flagged by k_adj_flags and swept by a warp each: lane l takes the
+// candidates b + l, b + l + 32, ... of each stencil row, in order, and the
+// lanes' partial sums are folded by a fixed butterfly; lane 0 writes.  The
+// thread sweeps skip flagged particles.  The sums run in another order than
+// the thread's, so the two agree to rounding, not bitwise; both are
+// deterministic.
+
+template <class Ctr, class F>
+__device__ __forceinline__ void warp_visit(uint32_t i, Ctr&& ctr, const DevConsts& c,
+                                           const int32_t* __restrict__ cstart,
+                                           const int32_t* __restrict__ cend, uint32_t lane,
+                                           F&& f) {
+    Runs r;
+    runs_of(ctr(), c, cstart, cend, r);
+#pragma unroll 1
+    for (int o = 0; o < 9; ++o)
+#pragma unroll 1
+        for (int32_t j = r.b[o] + (int32_t)lane; j < r.e[o]; j += 32)
+            if ((uint32_t)j != i) f((uint32_t)j);
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+__device__ __forceinline__ float3 warp_sum(float3 v) {
+    return make_float3(warp_sum(v.x), warp_sum(v.y), warp_sum(v.z));
+}
+
+// The particles of one substep swept by warps (flag == nullptr: none).
+struct Heavy {
+    const uint8_t* flag;    // [n] 1: flagged (sorted index)
+    const uint32_t* list;   // the flagged particles, in no fixed order
+    const uint32_t* count;  // how many
+};
+
+// Warps per launch of the warp sweeps (4 blocks of 8 warps on each of 152 SMs);
+// each takes flagged particles in turn.
+constexpr unsigned kAdjWarpBlocks = 608;
+constexpr uint32_t kAdjNoWarps = 0xFFFFFFFFu;  // warp_above: no particle gets a warp
+constexpr uint32_t kAdjWarpAbove = 512;        // warp_above when the tuning gives 0
+
 // Constants of particle `id` (scene lookup by id for batches).
 template <class CP>
 __device__ __forceinline__ const DevConsts& consts_of(const CP& cp, uint32_t id) {
@@ -264,20 +317,57 @@ __device__ __forceinline__ const DevConsts& consts_of(const CP& cp, uint32_t id)
 // ---- reverse kernels --------------------------------------------------------------
 
 // Per substep: irr[i] = 1 when particle i's stencil centre is not its key
-// cell (predicted outside the grid); *any set when some particle is.
+// cell (predicted outside the grid), and word[0] set when some particle is;
+// with `above` != kAdjNoWarps, heavy[i] = 1 when i's key-cell stencil holds
+// more than `above` candidates, those particles listed (in no fixed order:
+// each one's result does not depend on it) and counted in word[1].
 template <class CP>
 __global__ void __launch_bounds__(kAdjBlock)
 k_adj_flags(const uint32_t* __restrict__ perm, const float4* __restrict__ XPc,
-            uint8_t* __restrict__ irr, uint32_t* __restrict__ any, uint32_t n, CP cp) {
+            const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
+            uint32_t above, uint8_t* __restrict__ irr, uint8_t* __restrict__ heavy,
+            uint32_t* __restrict__ list, uint32_t* __restrict__ word, uint32_t n, CP cp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const DevConsts& c = consts_of(cp, perm[i]);
-    const int3 a = stencil_centre(XPc[i], c), b = key_cell(XPc[i], c);
+    const float4 q = XPc[i];
+    const int3 a = stencil_centre(q, c), b = key_cell(q, c);
     const bool odd = a.x != b.x || a.y != b.y || a.z != b.z;
     irr[i] = odd ? 1 : 0;
-    if (odd) atomicOr(any, 1u);
+    if (odd) atomicOr(word, 1u);
+    if (above == kAdjNoWarps) return;
+    Runs r;
+    runs_of(b, c, cstart, cend, r);
+    uint32_t cand = 0;
+#pragma unroll
+    for (int o = 0; o < 9; ++o) cand += (uint32_t)(r.e[o] - r.b[o]);
+    const bool h = cand > above;
+    heavy[i] = h ? 1 : 0;
+    if (h) {
+        const uint32_t k = atomicAdd(word + 1, 1u);
+        if (check_ok(c, k < n)) list[k] = i;
+    }
 }
 
+// One neighbour reversal (Body::run<W>): blocks below `tblocks` take a
+// thread per unflagged particle, the blocks after them a warp per flagged
+// particle (in turn, from the list).
+template <class Body>
+__global__ void __launch_bounds__(kAdjBlock) k_adj_sweep(Body b, Heavy hv, uint32_t n,
+                                                         uint32_t tblocks) {
+    if (blockIdx.x < tblocks) {
+        const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i >= n || (hv.flag && hv.flag[i])) return;
+        b.template run<false>(i, 0u);
+        return;
+    }
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t w = ((blockIdx.x - tblocks) * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = ((gridDim.x - tblocks) * blockDim.x) >> 5;
+    const uint32_t cnt = min(*hv.count, n);
+#pragma unroll 1
+    for (uint32_t k = w; k < cnt; k += nw) b.template run<true>(hv.list[k], lane);
+}
 
 // vorticity.glsl:76-85 reversed, pointwise: from vf-bar to vs-bar, eta-bar and
 // the direct part of w-bar; accumulates d/d(eps_v).
@@ -312,84 +402,121 @@ k_adj_vort_b1(const uint32_t* __restrict__ perm, const float4* __restrict__ VB,
 // vorticity.glsl:65-74 reversed: eta_i = sum_j |w_j| G_ij.  Gathers |w|-bar
 // and the position adjoint, then folds |w|-bar into w-bar.
 template <class CP>
-__global__ void __launch_bounds__(kAdjBlock)
-k_adj_vort_b2(const uint32_t* __restrict__ perm, const float4* __restrict__ XPc,
-              const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
-              const float4* __restrict__ Q, const float4* __restrict__ OM,
-              const float4* __restrict__ ETB, float4* __restrict__ OMB, float4* __restrict__ PA,
-              AdjLists al, PairDirs dirs, uint32_t n, CP cp) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t id = perm[i];
-    const DevConsts& c = consts_of(cp, id);
-    const float4 Qi = Q[i];
-    const float3 pi = f3(Qi);
-    const float mi = Qi.w;
-    const float3 ebi = f3(ETB[i]);
-    float mb = 0.0f;
-    float3 pb = make_float3(0.0f, 0.0f, 0.0f);
-    adj_scan_eval(i, [&] { return key_cell(XPc[i], c); }, c, cstart, cend, Q, pi, al, [&](uint32_t j) {
-        const float4 Qj = __ldg(Q + j);
-        const float3 d = pi - f3(Qj);
-        const float r2 = dotf(d, d);
-        if (r2 > c.r2cut || r2 == 0.0f) return;
-        const Spiky sp(c, sqrtf(r2));
-        float own, trans;
-        dirs.of(c, i, j, own, trans);
-        const float3 ebj = trans * f3(__ldg(ETB + j));
-        mb -= dotf(ebj, sp.G(d));
-        pb = pb + sp.H(d, (own * Qj.w) * ebi - mi * ebj);
-    });
-    float3 wb = f3(OMB[i]);
-    if (mi > 0.0f) wb = wb + (mb / mi) * f3(OM[i]);
-    OMB[i] = make_float4(wb.x, wb.y, wb.z, 0.0f);
-    PA[i] = make_float4(pb.x, pb.y, pb.z, 0.0f);
-}
+struct AdjVortB2 {
+    const uint32_t* __restrict__ perm;
+    const float4* __restrict__ XPc;
+    const int32_t* __restrict__ cstart;
+    const int32_t* __restrict__ cend;
+    const float4* __restrict__ Q;
+    const float4* __restrict__ OM;
+    const float4* __restrict__ ETB;
+    float4* __restrict__ OMB;
+    float4* __restrict__ PA;
+    AdjLists al;
+    PairDirs dirs;
+    CP cp;
+    template <bool W>
+    __device__ __forceinline__ void run(uint32_t i, uint32_t lane) const {
+        const uint32_t id = perm[i];
+        const DevConsts& c = consts_of(cp, id);
+        const float4 Qi = Q[i];
+        const float3 pi = f3(Qi);
+        const float mi = Qi.w;
+        const float3 ebi = f3(ETB[i]);
+        float mb = 0.0f;
+        float3 pb = make_float3(0.0f, 0.0f, 0.0f);
+        auto ctr = [&] { return key_cell(XPc[i], c); };
+        auto pair = [&](uint32_t j) {
+            const float4 Qj = __ldg(Q + j);
+            const float3 d = pi - f3(Qj);
+            const float r2 = dotf(d, d);
+            if (r2 > c.r2cut || r2 == 0.0f) return;
+            const Spiky sp(c, sqrtf(r2));
+            float own, trans;
+            dirs.of(c, i, j, own, trans);
+            const float3 ebj = trans * f3(__ldg(ETB + j));
+            mb -= dotf(ebj, sp.G(d));
+            pb = pb + sp.H(d, (own * Qj.w) * ebi - mi * ebj);
+        };
+        if constexpr (W) {
+            warp_visit(i, ctr, c, cstart, cend, lane, pair);
+            mb = warp_sum(mb);
+            pb = warp_sum(pb);
+            if (lane) return;
+        } else {
+            adj_scan_eval(i, ctr, c, cstart, cend, Q, pi, al, pair);
+        }
+        float3 wb = f3(OMB[i]);
+        if (mi > 0.0f) wb = wb + (mb / mi) * f3(OM[i]);
+        OMB[i] = make_float4(wb.x, wb.y, wb.z, 0.0f);
+        PA[i] = make_float4(pb.x, pb.y, pb.z, 0.0f);
+    }
+};
 
 // vorticity.glsl:47-58 reversed (XSPH and the vorticity vector): gathers the
 // committed-velocity adjoint and adds the position adjoint; accumulates d/dc.
 template <class CP>
-__global__ void __launch_bounds__(kAdjBlock)
-k_adj_vort_a(const uint32_t* __restrict__ perm, const float4* __restrict__ XPc,
-             const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
-             const float4* __restrict__ PF, const float4* __restrict__ VS,
-             const float4* __restrict__ VSB, const float4* __restrict__ OMB,
-             float4* __restrict__ VCB, float4* __restrict__ PA, double* __restrict__ acc_c,
-             AdjLists al, PairDirs dirs, uint32_t n, CP cp) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t id = perm[i];
-    const DevConsts& c = consts_of(cp, id);
-    const float3 pi = f3(PF[i]);
-    const float3 vi = f3(VS[i]);
-    const float3 sbi = f3(VSB[i]);
-    const float3 wbi = f3(OMB[i]);
-    float3 vb = sbi;
-    float3 pb = f3(PA[i]);
-    float3 wsum = make_float3(0.0f, 0.0f, 0.0f);
-    adj_visit_again(i, [&] { return key_cell(XPc[i], c); }, c, cstart, cend, al, [&](uint32_t j) {
-        const float3 d = pi - f3(__ldg(PF + j));
-        const float r2 = dotf(d, d);
-        if (r2 > c.r2cut) return;
-        float own, trans;
-        dirs.of(c, i, j, own, trans);
-        const float3 vji = f3(__ldg(VS + j)) - vi;
-        const float3 sbj = trans * f3(__ldg(VSB + j));
-        const float3 sbo = own * sbi;
-        const float W = w6(c, r2);
-        vb = vb + (c.cx * W) * (sbj - sbo);
-        wsum = wsum + (own * W) * vji;
-        pb = pb + (c.cx * dotf(sbo - sbj, vji)) * w6_grad(c, d, r2);
-        if (r2 == 0.0f) return;
-        const Spiky sp(c, sqrtf(r2));
-        const float3 wbs = own * wbi + trans * f3(__ldg(OMB + j));
-        vb = vb - crossf(sp.G(d), wbs);
-        pb = pb + sp.H(d, crossf(wbs, vji));
-    });
-    acc_c[id] += (double)dotf(sbi, wsum);
-    VCB[i] = make_float4(vb.x, vb.y, vb.z, 0.0f);
-    PA[i] = make_float4(pb.x, pb.y, pb.z, 0.0f);
-}
+struct AdjVortA {
+    const uint32_t* __restrict__ perm;
+    const float4* __restrict__ XPc;
+    const int32_t* __restrict__ cstart;
+    const int32_t* __restrict__ cend;
+    const float4* __restrict__ PF;
+    const float4* __restrict__ VS;
+    const float4* __restrict__ VSB;
+    const float4* __restrict__ OMB;
+    float4* __restrict__ VCB;
+    float4* __restrict__ PA;
+    double* __restrict__ acc_c;
+    AdjLists al;
+    PairDirs dirs;
+    CP cp;
+    template <bool W>
+    __device__ __forceinline__ void run(uint32_t i, uint32_t lane) const {
+        const uint32_t id = perm[i];
+        const DevConsts& c = consts_of(cp, id);
+        const float3 pi = f3(PF[i]);
+        const float3 vi = f3(VS[i]);
+        const float3 sbi = f3(VSB[i]);
+        const float3 wbi = f3(OMB[i]);
+        const float3 zero = make_float3(0.0f, 0.0f, 0.0f);
+        float3 vb = W ? zero : sbi;
+        float3 pb = W ? zero : f3(PA[i]);
+        float3 wsum = zero;
+        auto ctr = [&] { return key_cell(XPc[i], c); };
+        auto pair = [&](uint32_t j) {
+            const float3 d = pi - f3(__ldg(PF + j));
+            const float r2 = dotf(d, d);
+            if (r2 > c.r2cut) return;
+            float own, trans;
+            dirs.of(c, i, j, own, trans);
+            const float3 vji = f3(__ldg(VS + j)) - vi;
+            const float3 sbj = trans * f3(__ldg(VSB + j));
+            const float3 sbo = own * sbi;
+            const float W6 = w6(c, r2);
+            vb = vb + (c.cx * W6) * (sbj - sbo);
+            wsum = wsum + (own * W6) * vji;
+            pb = pb + (c.cx * dotf(sbo - sbj, vji)) * w6_grad(c, d, r2);
+            if (r2 == 0.0f) return;
+            const Spiky sp(c, sqrtf(r2));
+            const float3 wbs = own * wbi + trans * f3(__ldg(OMB + j));
+            vb = vb - crossf(sp.G(d), wbs);
+            pb = pb + sp.H(d, crossf(wbs, vji));
+        };
+        if constexpr (W) {
+            warp_visit(i, ctr, c, cstart, cend, lane, pair);
+            vb = sbi + warp_sum(vb);
+            pb = f3(PA[i]) + warp_sum(pb);
+            wsum = warp_sum(wsum);
+            if (lane) return;
+        } else {
+            adj_visit_again(i, ctr, c, cstart, cend, al, pair);
+        }
+        acc_c[id] += (double)dotf(sbi, wsum);
+        VCB[i] = make_float4(vb.x, vb.y, vb.z, 0.0f);
+        PA[i] = make_float4(pb.x, pb.y, pb.z, 0.0f);
+    }
+};
 
 // update.glsl:23-27 reversed: p-bar of the final positions, x_old-bar, and
 // the clamp mask of the last solver iteration.
@@ -422,97 +549,133 @@ k_adj_commit(const uint32_t* __restrict__ perm, const float4* __restrict__ XB,
 // calclambda's reverse: writes p-bar of the delta-p terms and (rho-bar, S-bar);
 // accumulates d/d(eps) and d/dk.
 template <class CP>
-__global__ void __launch_bounds__(kAdjBlock)
-k_adj_delta_p(const uint32_t* __restrict__ perm, const float4* __restrict__ XPc,
-              const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
-              const float4* __restrict__ L, const float4* __restrict__ AUX,
-              const float4* __restrict__ QB, float4* __restrict__ PDB, float4* __restrict__ RS,
-              double* __restrict__ acc_eps, double* __restrict__ acc_k, AdjLists al,
-              PairDirs dirs, uint32_t n, CP cp) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t id = perm[i];
-    const DevConsts& c = consts_of(cp, id);
-    const float4 Li = L[i];
-    const float3 pi = f3(Li);
-    const float li = Li.w;
-    const float3 qbi = f3(QB[i]);
-    float lb = 0.0f, kb = 0.0f;
-    float3 pb = qbi;
-    const float sc4 = c.scale * c.scale * c.scale * c.scale;
-    adj_scan_eval(i, [&] { return key_cell(XPc[i], c); }, c, cstart, cend, L, pi, al, [&](uint32_t j) {
-        const float4 Lj = __ldg(L + j);
-        const float3 d = pi - f3(Lj);
-        const float r2 = dotf(d, d);
-        if (r2 > c.r2cut || r2 == 0.0f) return;
-        const Spiky sp(c, sqrtf(r2));
-        const float t = c.h2 - r2;
-        const float W = c.k6 * t * t * t;
-        const float W3 = W * W * W;
-        const float s = c.negk * sc4 * W3 * W;
-        const float a = (li + Lj.w + s) * c.oorho;
-        const float3 G = sp.G(d);
-        float own, trans;
-        dirs.of(c, i, j, own, trans);
-        const float3 dq = own * qbi - trans * f3(__ldg(QB + j));
-        const float dqG = dotf(dq, G);
-        lb += c.oorho * dqG;
-        // (ds/dr)/r = 4 negk scale^4 W^3 (-6 k6 (h^2 - r^2)^2)
-        const float sr = 4.0f * c.negk * sc4 * W3 * (-6.0f * c.k6 * t * t);
-        pb = pb + sp.H(d, a * dq) + (c.oorho * sr * dqG) * d;
-        kb -= own * c.oorho * dotf(qbi, G) * sc4 * W3 * W;
-    });
-    const float4 aux = AUX[i];
-    const float D = aux.w + c.eps;
-    const float rb = -lb * c.oorho / D;
-    const float Sb = -lb * li / D;
-    acc_eps[id] += (double)Sb;
-    acc_k[id] += (double)kb;
-    PDB[i] = make_float4(pb.x, pb.y, pb.z, 0.0f);
-    RS[i] = make_float4(rb, Sb, 0.0f, 0.0f);
-}
+struct AdjDeltaP {
+    const uint32_t* __restrict__ perm;
+    const float4* __restrict__ XPc;
+    const int32_t* __restrict__ cstart;
+    const int32_t* __restrict__ cend;
+    const float4* __restrict__ L;
+    const float4* __restrict__ AUX;
+    const float4* __restrict__ QB;
+    float4* __restrict__ PDB;
+    float4* __restrict__ RS;
+    double* __restrict__ acc_eps;
+    double* __restrict__ acc_k;
+    AdjLists al;
+    PairDirs dirs;
+    CP cp;
+    template <bool W>
+    __device__ __forceinline__ void run(uint32_t i, uint32_t lane) const {
+        const uint32_t id = perm[i];
+        const DevConsts& c = consts_of(cp, id);
+        const float4 Li = L[i];
+        const float3 pi = f3(Li);
+        const float li = Li.w;
+        const float3 qbi = f3(QB[i]);
+        float lb = 0.0f, kb = 0.0f;
+        float3 pb = W ? make_float3(0.0f, 0.0f, 0.0f) : qbi;
+        const float sc4 = c.scale * c.scale * c.scale * c.scale;
+        auto ctr = [&] { return key_cell(XPc[i], c); };
+        auto pair = [&](uint32_t j) {
+            const float4 Lj = __ldg(L + j);
+            const float3 d = pi - f3(Lj);
+            const float r2 = dotf(d, d);
+            if (r2 > c.r2cut || r2 == 0.0f) return;
+            const Spiky sp(c, sqrtf(r2));
+            const float t = c.h2 - r2;
+            const float W6 = c.k6 * t * t * t;
+            const float W3 = W6 * W6 * W6;
+            const float s = c.negk * sc4 * W3 * W6;
+            const float a = (li + Lj.w + s) * c.oorho;
+            const float3 G = sp.G(d);
+            float own, trans;
+            dirs.of(c, i, j, own, trans);
+            const float3 dq = own * qbi - trans * f3(__ldg(QB + j));
+            const float dqG = dotf(dq, G);
+            lb += c.oorho * dqG;
+            // (ds/dr)/r = 4 negk scale^4 W^3 (-6 k6 (h^2 - r^2)^2)
+            const float sr = 4.0f * c.negk * sc4 * W3 * (-6.0f * c.k6 * t * t);
+            pb = pb + sp.H(d, a * dq) + (c.oorho * sr * dqG) * d;
+            kb -= own * c.oorho * dotf(qbi, G) * sc4 * W3 * W6;
+        };
+        if constexpr (W) {
+            warp_visit(i, ctr, c, cstart, cend, lane, pair);
+            lb = warp_sum(lb);
+            kb = warp_sum(kb);
+            pb = qbi + warp_sum(pb);
+            if (lane) return;
+        } else {
+            adj_scan_eval(i, ctr, c, cstart, cend, L, pi, al, pair);
+        }
+        const float4 aux = AUX[i];
+        const float D = aux.w + c.eps;
+        const float rb = -lb * c.oorho / D;
+        const float Sb = -lb * li / D;
+        acc_eps[id] += (double)Sb;
+        acc_k[id] += (double)kb;
+        PDB[i] = make_float4(pb.x, pb.y, pb.z, 0.0f);
+        RS[i] = make_float4(rb, Sb, 0.0f, 0.0f);
+    }
+};
 
 // calclambda.glsl:75-101 reversed (one iteration): gathers the density and
 // denominator terms; masks the previous iteration's clamp, or un-sorts into
 // the predicted-position adjoint after the first iteration.
 template <class CP>
-__global__ void __launch_bounds__(kAdjBlock)
-k_adj_lambda(const uint32_t* __restrict__ perm, const float4* __restrict__ XPc,
-             const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
-             const float4* __restrict__ L, const float4* __restrict__ AUX,
-             const float4* __restrict__ RS, const float4* __restrict__ PDB,
-             float4* __restrict__ QB, float4* __restrict__ XSB, int first, AdjLists al,
-             PairDirs dirs, uint32_t n, CP cp) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t id = perm[i];
-    const DevConsts& c = consts_of(cp, id);
-    const float3 pi = f3(L[i]);
-    const float4 RSi = RS[i];
-    const float3 gi = f3(AUX[i]);
-    float3 pb = f3(PDB[i]);
-    adj_visit_again(i, [&] { return key_cell(XPc[i], c); }, c, cstart, cend, al, [&](uint32_t j) {
-        const float3 d = pi - f3(__ldg(L + j));
-        const float r2 = dotf(d, d);
-        if (r2 > c.r2cut) return;
-        float own, trans;
-        dirs.of(c, i, j, own, trans);
-        const float4 RSj = __ldg(RS + j);
-        pb = pb + (own * RSi.x + trans * RSj.x) * w6_grad(c, d, r2);
-        if (r2 == 0.0f) return;
-        const Spiky sp(c, sqrtf(r2));
-        const float3 gij = c.oorho * sp.G(d);
-        const float3 gj = f3(__ldg(AUX + j));
-        const float3 u = (own * RSi.y) * (gij + gi) + (trans * RSj.y) * (gij - gj);
-        pb = pb + (2.0f * c.oorho) * sp.H(d, u);
-    });
-    if (first) {
-        XSB[id] = make_float4(pb.x, pb.y, pb.z, 0.0f);
-    } else {
-        pb = clamp_mask(pb, pi, c);
-        QB[i] = make_float4(pb.x, pb.y, pb.z, 0.0f);
+struct AdjLambda {
+    const uint32_t* __restrict__ perm;
+    const float4* __restrict__ XPc;
+    const int32_t* __restrict__ cstart;
+    const int32_t* __restrict__ cend;
+    const float4* __restrict__ L;
+    const float4* __restrict__ AUX;
+    const float4* __restrict__ RS;
+    const float4* __restrict__ PDB;
+    float4* __restrict__ QB;
+    float4* __restrict__ XSB;
+    int first;
+    AdjLists al;
+    PairDirs dirs;
+    CP cp;
+    template <bool W>
+    __device__ __forceinline__ void run(uint32_t i, uint32_t lane) const {
+        const uint32_t id = perm[i];
+        const DevConsts& c = consts_of(cp, id);
+        const float3 pi = f3(L[i]);
+        const float4 RSi = RS[i];
+        const float3 gi = f3(AUX[i]);
+        float3 pb = W ? make_float3(0.0f, 0.0f, 0.0f) : f3(PDB[i]);
+        auto ctr = [&] { return key_cell(XPc[i], c); };
+        auto pair = [&](uint32_t j) {
+            const float3 d = pi - f3(__ldg(L + j));
+            const float r2 = dotf(d, d);
+            if (r2 > c.r2cut) return;
+            float own, trans;
+            dirs.of(c, i, j, own, trans);
+            const float4 RSj = __ldg(RS + j);
+            pb = pb + (own * RSi.x + trans * RSj.x) * w6_grad(c, d, r2);
+            if (r2 == 0.0f) return;
+            const Spiky sp(c, sqrtf(r2));
+            const float3 gij = c.oorho * sp.G(d);
+            const float3 gj = f3(__ldg(AUX + j));
+            const float3 u = (own * RSi.y) * (gij + gi) + (trans * RSj.y) * (gij - gj);
+            pb = pb + (2.0f * c.oorho) * sp.H(d, u);
+        };
+        if constexpr (W) {
+            warp_visit(i, ctr, c, cstart, cend, lane, pair);
+            pb = f3(PDB[i]) + warp_sum(pb);
+            if (lane) return;
+        } else {
+            adj_visit_again(i, ctr, c, cstart, cend, al, pair);
+        }
+        if (first) {
+            XSB[id] = make_float4(pb.x, pb.y, pb.z, 0.0f);
+        } else {
+            pb = clamp_mask(pb, pi, c);
+            QB[i] = make_float4(pb.x, pb.y, pb.z, 0.0f);
+        }
     }
-}
+};
 
 // predictpos.glsl:32-34 reversed: x* = x + dt v'; plus the commit's x_old.
 template <class CP>
@@ -574,7 +737,9 @@ cudaError_t alloc_tape(pbf_sim* s, Tape* t) {
         if (e == cudaSuccess) e = talloc(t, w, n);
     if (e == cudaSuccess) e = talloc(t, &t->acc, (size_t)kParams * n);
     if (e == cudaSuccess) e = talloc(t, &t->irr, n);
-    if (e == cudaSuccess) e = talloc(t, &t->any_irr, 1);
+    if (e == cudaSuccess) e = talloc(t, &t->words, 2);
+    if (e == cudaSuccess) e = talloc(t, &t->heavy, n);
+    if (e == cudaSuccess) e = talloc(t, &t->heavy_list, n);
     return e;
 }
 
@@ -593,27 +758,32 @@ cudaError_t reverse_substep(pbf_sim* s, Tape* t, const Tape::Slot& sl, const CP&
     // centred (neighbourcells.glsl:57): the first lambda sweep's L holds them,
     // and PF does when there is no solver iteration
     const float4* XPc = iters > 0 ? sl.L[0] : sl.PF;
-    cudaError_t fe = cudaMemsetAsync(t->any_irr, 0, sizeof(uint32_t), st);
+    cudaError_t fe = cudaMemsetAsync(t->words, 0, 2 * sizeof(uint32_t), st);
     if (fe != cudaSuccess) return fe;
-    k_adj_flags<<<g, kAdjBlock, 0, st>>>(sl.perm, XPc, t->irr, t->any_irr, n, cp);
-    const PairDirs dirs{t->irr, XPc, t->any_irr};
+    k_adj_flags<<<g, kAdjBlock, 0, st>>>(sl.perm, XPc, sl.cstart, sl.cend, t->warp_above, t->irr,
+                                         t->heavy, t->heavy_list, t->words, n, cp);
+    const PairDirs dirs{t->irr, XPc, t->words};
+    // the particles with dense stencils get a warp each
+    const bool warps = t->warp_above != kAdjNoWarps;
+    const Heavy hv{warps ? t->heavy : nullptr, t->heavy_list, t->words + 1};
+    auto sweep = [&](const auto& body) {
+        k_adj_sweep<<<g + (warps ? kAdjWarpBlocks : 0u), kAdjBlock, 0, st>>>(body, hv, n, g);
+    };
     if (t->vort) {
         k_adj_vort_b1<<<g, kAdjBlock, 0, st>>>(sl.perm, t->VB, sl.OM, sl.ETA, t->VSB, t->ETB,
                                                t->OMB, acc_ev, n, cp);
-        k_adj_vort_b2<<<g, kAdjBlock, 0, st>>>(sl.perm, XPc, sl.cstart, sl.cend, sl.Q, sl.OM,
-                                               t->ETB, t->OMB, t->PA, al, dirs, n, cp);
-        k_adj_vort_a<<<g, kAdjBlock, 0, st>>>(sl.perm, XPc, sl.cstart, sl.cend, sl.PF, sl.VS,
-                                              t->VSB, t->OMB, t->VCB, t->PA, acc_c, al, dirs, n, cp);
+        sweep(AdjVortB2<CP>{sl.perm, XPc, sl.cstart, sl.cend, sl.Q, sl.OM, t->ETB, t->OMB, t->PA,
+                            al, dirs, cp});
+        sweep(AdjVortA<CP>{sl.perm, XPc, sl.cstart, sl.cend, sl.PF, sl.VS, t->VSB, t->OMB,
+                           t->VCB, t->PA, acc_c, al, dirs, cp});
     }
     k_adj_commit<<<g, kAdjBlock, 0, st>>>(sl.perm, t->XB, t->VB, t->VCB, t->PA, sl.PF, t->QB,
                                           t->XOB, t->XSB, t->vort ? 1 : 0, iters, n, cp);
     for (int k = iters - 1; k >= 0; --k) {
-        k_adj_delta_p<<<g, kAdjBlock, 0, st>>>(sl.perm, XPc, sl.cstart, sl.cend, sl.L[k],
-                                               sl.AUX[k], t->QB, t->PDB, t->RS, acc_eps, acc_k, al,
-                                               dirs, n, cp);
-        k_adj_lambda<<<g, kAdjBlock, 0, st>>>(sl.perm, XPc, sl.cstart, sl.cend, sl.L[k],
-                                              sl.AUX[k], t->RS, t->PDB, t->QB, t->XSB,
-                                              k == 0 ? 1 : 0, al, dirs, n, cp);
+        sweep(AdjDeltaP<CP>{sl.perm, XPc, sl.cstart, sl.cend, sl.L[k], sl.AUX[k], t->QB, t->PDB,
+                            t->RS, acc_eps, acc_k, al, dirs, cp});
+        sweep(AdjLambda<CP>{sl.perm, XPc, sl.cstart, sl.cend, sl.L[k], sl.AUX[k], t->RS, t->PDB,
+                            t->QB, t->XSB, k == 0 ? 1 : 0, al, dirs, cp});
     }
     k_adj_predict<<<g, kAdjBlock, 0, st>>>(t->XSB, t->XOB, t->XB2, t->VB2, n, cp);
     std::swap(t->XB, t->XB2);
@@ -732,6 +902,8 @@ pbf_status pbf_backward(pbf_sim* s, const float* dL_dx4, const float* dL_dv4, in
     PBF_CUDA(s, cudaMemsetAsync(t->acc, 0, sizeof(double) * kParams * n, st));
     PBF_CUDA(s, cudaMemsetAsync(t->VCB, 0, b, st));
     PBF_CUDA(s, cudaMemsetAsync(t->PA, 0, b, st));
+    t->warp_above = s->tuning.adjoint_warp_candidates ? s->tuning.adjoint_warp_candidates
+                                                      : kAdjWarpAbove;
     const uint32_t nseg = (t->substeps + t->every - 1) / t->every;
     for (int seg = (int)nseg - 1; seg >= 0; --seg) {
         const uint32_t t0 = (uint32_t)seg * t->every;

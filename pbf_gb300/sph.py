@@ -174,7 +174,8 @@ class SPH:
 
     def set_tuning(self, use_neighbour_lists=None, list_capacity=None, skin_h=None,
                    block_size=None, sweep_mode=None, pair_list_capacity=None,
-                   coop_candidates=None, auto_period=None) -> None:
+                   coop_candidates=None, auto_period=None,
+                   adjoint_warp_candidates=None) -> None:
         t = self.get_tuning()
         if use_neighbour_lists is not None:
             t.use_neighbour_lists = 1 if use_neighbour_lists else 0
@@ -194,6 +195,8 @@ class SPH:
             t.coop_candidates = int(coop_candidates)
         if auto_period is not None:
             t.auto_period = int(auto_period)
+        if adjoint_warp_candidates is not None:
+            t.adjoint_warp_candidates = int(adjoint_warp_candidates)
         check(self._lib.pbf_set_tuning(self._h, C.byref(t)), self._h)
 
     PASSES = ("masked", "direct", "coop", "direct+coop", "mixed")

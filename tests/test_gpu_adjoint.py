@@ -221,3 +221,45 @@ def test_adjoint_with_stencils_outside_the_grid(gpu, oracle_mod):
     ref = np.einsum("nc,knc->k", w[:, :3].astype(np.float64), xd)
     g = [dv0[i, c] for i, c in coords] + [dx0[i, c] for i, c in coords[:4]] + list(gp)
     check(g, ref, "gradients with stencils outside the grid")
+
+
+def test_warp_sweeps_match_thread_sweeps(gpu):
+    """Collapsed state: the 32,768-particle epsilon = 0.01 run after 40
+    substeps holds most particles in coincident piles of 32 or more.  From
+    those positions at rest, with epsilon = 5, the reverse sweeps that give
+    each particle with a dense stencil a warp (its pair terms summed across
+    the lanes) agree with the thread-per-particle sweeps.  The sums run in
+    another order (thousands of terms in float), so the two agree to 1e-3 of
+    the largest component, not bitwise; each is deterministic."""
+    a, _ = scenes.diff_32k()
+    n = a.n
+    sim = pg.SPH(n, tuple(a.params.grid), a.params)
+    sim.set_state(a.x4, a.v4)
+    sim.step(40)
+    x0, _ = sim.get_state()
+    _, cnt = np.unique(x0[:, :3], axis=0, return_counts=True)
+    assert cnt[cnt >= 32].sum() > n // 2 and cnt.max() >= 1000  # the piles exist
+    v0 = np.zeros_like(x0)
+    p = a.params.copy()
+    p.epsilon = 5.0
+    sim.set_params(p)
+    rng = np.random.default_rng(3)
+    w = rng.normal(size=(n, 4)).astype(np.float32)
+    u = rng.normal(size=(n, 4)).astype(np.float32)
+    w[:, 3] = 0
+    u[:, 3] = 0
+    out = []
+    for warp_above in (0xFFFFFFFF, 0, 0):
+        sim.set_tuning(adjoint_warp_candidates=warp_above)
+        sim.set_state(x0, v0)
+        sim.forward_record(4, 2)
+        out.append(sim.backward(w, u))
+    (dx_t, dv_t, g_t), (dx_w, dv_w, g_w), (dx_w2, dv_w2, g_w2) = out
+    assert np.array_equal(dx_w, dx_w2) and np.array_equal(dv_w, dv_w2)  # deterministic
+    assert np.array_equal(g_w, g_w2)
+    for name, got, want in (("dL/dx0", dx_w, dx_t), ("dL/dv0", dv_w, dv_t)):
+        assert np.all(np.isfinite(want[:, :3])), name
+        scale = float(np.abs(want[:, :3]).max())
+        err = float(np.abs(got[:, :3] - want[:, :3]).max())
+        assert err <= 1e-3 * scale, (name, err, scale)
+    np.testing.assert_allclose(g_w, g_t, rtol=1e-3, atol=1e-6 * float(np.abs(g_t).max()))
