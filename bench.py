@@ -26,10 +26,10 @@ flushed between steps.
 
 --impl reference times the reference path on the host cores instead: the
 oracle (a C++ restatement of pbf's GLSL compute shaders, OpenMP; the
-reference itself needs an OpenGL 4.3 context, which these machines lack).
-Each of its steps is a bounded sample of one substep: predict, sort and
-cell ranges over all particles plus the neighbour stages over a slice of
-the sorted particles, extrapolated to the full substep.
+reference itself needs an OpenGL 4.3 context, which these machines lack),
+W warm-up substeps, then the same window (substeps 1..K from the initial
+scene), every substep in full, as many whole substeps as fit in about four
+minutes.
 """
 from __future__ import annotations
 
