@@ -88,7 +88,32 @@ def parse():
                     help="the default (kept for older command lines)")
     ap.add_argument("--no-recovery", action="store_true",
                     help="skip the 64-scene parameter recovery (about a minute)")
+    ap.add_argument("--substep-stages", type=int, default=0,
+                    help="instead of the benchmark: one JSON line per substep 1..N of the "
+                         "workload with its stage times (eager, CUDA events per stage)")
     return ap.parse_args()
+
+
+def substep_stages(scene, count: int) -> None:
+    """Stage milliseconds of each of the first `count` substeps of the
+    workload (after W = 5 warm-up substeps and a reset), from the stage
+    events of the eager timing mode (pbf_enable_timing), one JSON line each."""
+    import pbf_gb300 as pg
+    sim = pg.SPH(scene.n, tuple(scene.params.grid), scene.params)
+    sim.set_state(scene.x4, scene.v4)
+    sim.step(5)
+    sim.synchronize()
+    sim.set_state(scene.x4, scene.v4)
+    sim.EnableTiming(True)
+    prev = {k: 0.0 for k in pg.SPH.STAGES}
+    for k in range(1, count + 1):
+        sim.step(1)
+        st, _ = sim.stage_times()
+        d = {a: round(st[a] - prev[a], 3) for a in st}
+        prev = st
+        print(json.dumps({"substep": k, "total_ms": round(sum(d.values()), 3), **d,
+                          "solver_sweeps": sim.sweep_choice()["solver"]}), flush=True)
+    sim.close()
 
 
 def dist_env():
@@ -640,6 +665,9 @@ def main():
         return 0
     from pbf_gb300 import scenes
     scene = getattr(scenes, args.scene)()
+    if args.substep_stages > 0:
+        substep_stages(scene, args.substep_stages)
+        return 0
     if world > 1:
         # replicas: the window and e2e lines scale; the single-GPU legs
         # (full runs, batch, adjoint, splatting, the 16k configuration) would
