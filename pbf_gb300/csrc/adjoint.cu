@@ -10,8 +10,10 @@
 // Every reverse sweep is written as a gather, not a scatter: the pair
 // functions obey G(-d) = -G(d), H(-d) = H(d), W(-d) = W(d), so each particle
 // sums the contributions of its own equation and of its neighbours'
-// equations from per-particle adjoint quantities.  No atomics: results are
-// deterministic.  The candidate relation is symmetric except around particles
+// equations from per-particle adjoint quantities.  No atomic adds into any
+// sum (the only atomics set a flag and append to a list whose order no result
+// depends on): results are deterministic.  The candidate relation is
+// symmetric except around particles
 // predicted outside the grid: the forward centres a stencil on the unclamped
 // predicted cell (neighbourcells.glsl:57) while the sort files the particle
 // under its clamped cell, so such a particle i may be a candidate of j without
