@@ -232,7 +232,7 @@ typedef struct pbf_tuning {
     uint32_t adjoint_warp_candidates; /* pbf_backward: particles whose stencil holds more
                                      than this many candidates get a warp each in the
                                      reverse neighbour sweeps (their pair terms summed
-                                     across its lanes), the others a thread; 0 = 256;
+                                     across its lanes), the others a thread; 0 = 512;
                                      0xFFFFFFFF: a thread for every particle */
 } pbf_tuning;
 
