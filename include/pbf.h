@@ -37,9 +37,10 @@ extern "C" {
 #endif
 
 /* Bumped whenever a struct passed across the ABI changes layout (2: pbf_tuning
- * gained coop_candidates and auto_period).  A caller compiled against another
- * version must not pass its structs to this library. */
-#define PBF_ABI_VERSION 2
+ * gained coop_candidates and auto_period; 3: adjoint_warp_candidates).  A
+ * caller compiled against another version must not pass its structs to this
+ * library. */
+#define PBF_ABI_VERSION 3
 
 typedef enum pbf_status {
     PBF_OK = 0,
